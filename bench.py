@@ -1,0 +1,345 @@
+"""Benchmark of the Zeta device path on GB300.
+
+Default workload (one "step"): batched perft over 4096 seeded random
+playout positions (10-60 plies from the initial position, terminal
+positions discarded) at depths drawn uniformly from 3-5, in one persistent
+work-stealing launch sequence.  Metric: perft leaves per second, bit-exact
+(every step's counts are checked against the first step's).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the reference's own perft kernel (src/zetaperft.cl,
+compiled for the host from the unmodified source under a work-group
+emulator, oracle/_ref) on all host cores, on a bounded sample of the same
+workload.  Under torchrun each rank takes its own shard of positions
+(weak scaling; there is no device collective), rank 0 prints one JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "perft nodes/s (bit-exact)"
+UNIT = "leaves/s"
+WORKLOAD = "perft_batch"
+L2_FLUSH_BYTES = 256 << 20
+
+# Algorithmic 32-bit integer operations per node of the perft kernel
+# (u64 and/or/xor/not/add/sub/compare = 2, shift = 2 constant / 4 variable,
+# popc/ctz = 2), counted by zeta_gb300/csrc/opcount.cc on the initial
+# position's depth-5 tree with the kernel's own code; fixed, never retuned.
+OPS_PER_COUNTED_NODE = None  # filled from profiles/opcount.json when present
+OPS_PER_INTERIOR_NODE = None
+
+
+def _opcounts():
+    path = os.path.join(ROOT, "profiles", "opcount.json")
+    if os.path.exists(path):
+        d = json.load(open(path))
+        return d["ops_per_counted_node"], d["ops_per_interior_node"]
+    return None, None
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        return json.load(open(path))
+    return {}
+
+
+def workload_arrays(z, rank: int):
+    w = dict(z.WORKLOADS[WORKLOAD])
+    seed = w["seed"] + 0x1000003 * rank  # each rank its own shard
+    return z.make_positions(seed, w["n"], w["min_plies"], w["max_plies"], w["min_pieces"], w["min_depth"],
+                            w["max_depth"])
+
+
+def run_ours(args):
+    import torch
+    import zeta_gb300 as z
+
+    world, rank, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    z.init(local, 0, 0)
+    info = z.device_info()
+    boards, stm, depth = workload_arrays(z, rank)
+    n = len(depth)
+    dev = torch.device("cuda", local)
+    d_boards = torch.from_numpy(boards.view(np.int64)).to(dev)
+    d_stm = torch.from_numpy(stm).to(dev)
+    d_depth = torch.from_numpy(depth).to(dev)
+    d_leaves = torch.zeros(n, dtype=torch.int64, device=dev)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    sp = stream.cuda_stream
+
+    def step():
+        z.perft_batch_device(d_boards.data_ptr(), d_stm.data_ptr(), d_depth.data_ptr(), n, d_leaves.data_ptr(), sp)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    ref_counts = d_leaves.cpu().numpy().view(np.uint64).copy()
+
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    kernel_ms, counted, interior = [], 0, 0
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        for i in range(args.steps):
+            flush.fill_(i)  # write 256 MB (> L2) between timed steps
+            starts[i].record(stream)
+            step()
+            ends[i].record(stream)
+            st = z.perft_stats()
+            kernel_ms.append(st["kernel_ms"])
+            counted += st["counted_nodes"]
+            interior += st["interior_nodes"]
+            got = d_leaves.cpu().numpy().view(np.uint64)
+            if not np.array_equal(got, ref_counts):
+                raise SystemExit("perft counts changed between steps")
+        torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    total_s = sum(step_ms) / 1e3
+    leaves_rank = int(ref_counts.sum()) * args.steps
+    if world > 1:
+        t = torch.tensor([total_s], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_s = float(t.item())
+        c = torch.tensor([leaves_rank], dtype=torch.float64, device=dev)
+        dist.all_reduce(c)
+        leaves_all = float(c.item())
+    else:
+        leaves_all = float(leaves_rank)
+    value = leaves_all / total_s
+
+    # end to end: host buffers through the public C API (H2D + launch + D2H)
+    e2e_s = 0.0
+    for i in range(args.steps):
+        flush.fill_(i)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        out = z.perft_batch(boards, stm, depth)
+        e2e_s += time.perf_counter() - t0
+        if not np.array_equal(out, ref_counts):
+            raise SystemExit("host-buffer counts differ from device-buffer counts")
+    e2e_value = leaves_rank / e2e_s * (leaves_all / leaves_rank)
+
+    if rank != 0:
+        z.release()
+        return
+    peaks = measured_peaks()
+    ops_c, ops_i = _opcounts()
+    int_peak = None
+    try:
+        int_peak = z.int_peak_tops()
+    except Exception:  # noqa: BLE001 -- the microbenchmark is optional
+        int_peak = None
+    kernel_avg_ms = sum(kernel_ms) / len(kernel_ms)
+    roofline = None
+    if ops_c and int_peak:
+        ops = (counted / args.steps) * ops_c + (interior / args.steps) * ops_i
+        achieved = ops / (kernel_avg_ms / 1e3) / 1e12
+        traffic = None
+        tp = os.path.join(ROOT, "profiles", "perft_ws_traffic.json")
+        if os.path.exists(tp):
+            traffic = json.load(open(tp)).get("bytes_per_launch")
+        roofline = {"bound": "int32-alu", "achieved": round(achieved, 3), "peak": round(int_peak, 3),
+                    "unit": "Tops/s", "frac": round(achieved / int_peak, 4), "traffic": traffic,
+                    "peak_source": "measured: int32 LOP3/SHF/IADD3 microbenchmark (zeta_int_peak)",
+                    "kernel": "k_perft_ws"}
+    cpu = cpu_baseline_sample(boards, stm, depth)
+    line = {
+        "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(sum(step_ms) / len(step_ms), 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic (seeded random playouts)",
+        "config": {"workload": f"{WORKLOAD}: {n} seeded playouts of 10-60 plies, perft depth U[3,5]",
+                   "positions_per_gpu": n, "leaves_per_step_per_gpu": int(ref_counts.sum()),
+                   "l2": "flushed between timed steps (256 MB write)", "parallelism": f"replicas x{world}",
+                   "perft_config": z.perft_config()},
+        "e2e": {"value": round(e2e_value, 1), "unit": UNIT, "h2d_bytes_per_step": n * 58,
+                "d2h_bytes_per_step": n * 8},
+        "gpu_launches": 14 * args.steps,
+        "kernel_ms": round(kernel_avg_ms, 4),
+        "nodes": {"counted_per_step": counted // args.steps, "interior_per_step": interior // args.steps},
+        "roofline": roofline,
+        "cpu_baseline": cpu,
+        "clocks": clocks.summary(),
+        "device": {"sms": info["sms"], "cc": list(info["cc"]), "hbm_gbs_measured": peaks.get("hbm_gbs")},
+    }
+    print(json.dumps(line), flush=True)
+    z.release()
+
+
+def _ref_lib():
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib as ol
+    if ol.reference() is None:
+        return None, None
+    return ol, ol.reference()
+
+
+def cpu_baseline_sample(boards, stm, depth, budget_s: float = 12.0):
+    """The reference perft kernel on the host cores, on a bounded sample of
+    the workload: the first positions at depth 3 (leaves/s does not depend
+    on depth for a kernel that visits every leaf)."""
+    ol, ref = _ref_lib()
+    if ref is None:
+        return {"value": None, "unit": UNIT, "cores": 0, "kind": "reference",
+                "sample": "reference kernels not built on this host"}
+    cores = os.cpu_count() or 1
+    k = cores
+    total_leaves, total_s = 0, 0.0
+    while total_s < budget_s and k <= len(depth):
+        d3 = np.full(k, 3, dtype=np.int32)
+        t0 = time.perf_counter()
+        out = ol.ref_perft_batch(boards[:k], stm[:k], d3, cores)
+        dt = time.perf_counter() - t0
+        total_leaves, total_s = int(out.sum()), dt
+        if dt > budget_s / 3:
+            break
+        k = min(len(depth), k * 2) if k < len(depth) else k + 1
+    return {"value": round(total_leaves / total_s, 1), "unit": UNIT, "cores": cores, "kind": "reference",
+            "sample": f"unmodified zetaperft.cl on {cores} host threads (64-lane work-group emulator), "
+                      f"first {k} workload positions at depth 3, {total_leaves} leaves in {total_s:.1f}s"}
+
+
+def run_reference(args):
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return
+    ol, ref = _ref_lib()
+    if ref is None:
+        print(json.dumps({"impl": "reference", "unavailable": "reference kernels (oracle/_ref) not built here"}))
+        return
+    # the workload positions, made with the oracle's copy of the generator
+    import zeta_gb300 as zmod
+    w = dict(zmod.WORKLOADS[WORKLOAD])
+    boards, stm, depth = ol.make_positions(w["seed"], 256, min_plies=w["min_plies"], max_plies=w["max_plies"],
+                                           min_pieces=w["min_pieces"], min_depth=w["min_depth"],
+                                           max_depth=w["max_depth"])
+    cores = os.cpu_count() or 1
+    k = 2 * cores
+    d3 = np.full(k, 3, dtype=np.int32)
+    for _ in range(args.warmup):
+        ol.ref_perft_batch(boards[:cores], stm[:cores], d3[:cores], cores)
+    t_total, leaves = 0.0, 0
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        out = ol.ref_perft_batch(boards[:k], stm[:k], d3, cores)
+        t_total += time.perf_counter() - t0
+        leaves += int(out.sum())
+    value = leaves / t_total
+    sample = (f"unmodified zetaperft.cl on {cores} host threads, per step the first {k} workload positions "
+              f"at depth 3 ({leaves // args.steps} leaves)")
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t_total / args.steps * 1e3, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+        "data": "synthetic (seeded random playouts)",
+        "config": {"workload": f"{WORKLOAD}: seeded playouts of 10-60 plies (bounded sample at depth 3)"},
+        "cpu_baseline": {"value": round(value, 1), "unit": UNIT, "cores": cores, "kind": "reference",
+                         "sample": sample},
+        "e2e": {"value": round(value, 1), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

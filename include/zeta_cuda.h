@@ -1,0 +1,122 @@
+/*
+ * zeta_cuda.h -- C ABI of libzeta_cuda.so, the GB300 (sm_103a) device
+ * path of the Zeta chess engine.
+ *
+ * The reference drives its OpenCL kernels through six calls that pass all
+ * data in globals (src/clrun.h:25-30, src/zeta.h:35-139).  This library
+ * exposes the same work as explicit calls with plain pointers and sizes;
+ * include/clrun.h keeps the reference's six-call interface on top of it
+ * (zeta_gb300/host/cudarun.c).
+ *
+ * Conventions
+ *  - A board is the reference quad-bitboard, 7 x u64 (src/types.h:59-66):
+ *    [0] black pieces, [1..3] piece-type planes, [4] moved flags (castle
+ *    rights, en-passant target), [5] Zobrist hash, [6] half-move clock.
+ *  - Moves are the reference's 32-bit packing (src/types.h:67-74).
+ *  - Every call returns ZETA_OK (0) or a negative ZETA_ERR_* code; the
+ *    text of the last error is in zeta_last_error().  No call falls back
+ *    to the CPU: without a usable GB300 they fail.
+ *  - One host thread drives the library (as src/clrun.c assumes).
+ */
+#ifndef ZETA_CUDA_H
+#define ZETA_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ZETA_OK 0
+#define ZETA_ERR_CUDA -1       /* a CUDA runtime call failed */
+#define ZETA_ERR_ARG -2        /* bad argument (size, depth, pointer) */
+#define ZETA_ERR_STATE -3      /* zeta_init missing, or a second init */
+#define ZETA_ERR_CAPACITY -4   /* a work buffer was too small */
+#define ZETA_ERR_DEVICE -5     /* the kernel reported an error status */
+#define ZETA_ERR_BUDGET -6     /* a bounded device loop gave up */
+#define ZETA_ERR_NOALLOC -7    /* request exceeds a fixed-size static buffer */
+
+/* ------------------------------------------------------------------ */
+/* Device lifecycle.  Replaces cl_init_device / cl_release_device
+ * (src/clrun.c:51-514, 1268-1490).  tt1_mb / tt2_mb size the two
+ * transposition tables as the reference does (clrun.c:387-443: entries =
+ * largest power of two that fits); 0 disables a table. */
+int zeta_init(int device, uint64_t tt1_mb, uint64_t tt2_mb);
+int zeta_release(void);
+const char *zeta_last_error(void);
+
+/* Device facts the autotuner and the bench report. */
+int zeta_device_info(int *sm_count, int *cc_major, int *cc_minor, uint64_t *hbm_bytes);
+
+/* ------------------------------------------------------------------ */
+/* Perft (leaf count of the legal tree, queen-only promotions).
+ * Replaces cl_run_perft (src/clrun.c:979-1147) + the COUNTERS read-back
+ * and sum of src/search.c:225-271.  Host buffers. */
+int zeta_perft(const uint64_t board[7], int stm, int depth, uint64_t *leaves);
+
+/* n positions at once (one persistent work-stealing launch).
+ * boards: n*7 u64, stm/depth: n bytes, leaves: n u64.  Host buffers. */
+int zeta_perft_batch(const uint64_t *boards, const uint8_t *stm, const uint8_t *depth, int n,
+                     uint64_t *leaves);
+
+/* Same with DEVICE buffers already resident in HBM; enqueued on `stream`
+ * (a cudaStream_t, NULL = legacy default stream) and synchronised before
+ * returning.  Used to time the kernels without host copies. */
+int zeta_perft_batch_device(const uint64_t *d_boards, const uint8_t *d_stm, const uint8_t *d_depth,
+                            int n, uint64_t *d_leaves, void *stream);
+
+/* Launch geometry and split policy of the perft path (autotuner knobs).
+ * threads_per_block: 64..1024, multiple of 32; blocks_per_sm: 0 = from
+ * occupancy; min_tasks: split the tree until at least this many subtree
+ * tasks exist (0 = 4 x resident threads); task_depth: remaining depth of a
+ * subtree task, 1..3; use_graph: capture the launch sequence in a CUDA
+ * graph and replay it while the shapes stay the same. */
+typedef struct {
+  int threads_per_block;
+  int blocks_per_sm;
+  uint32_t min_tasks;
+  int task_depth;
+  int use_graph;
+} zeta_perft_config;
+int zeta_perft_configure(const zeta_perft_config *cfg);
+int zeta_perft_get_config(zeta_perft_config *cfg);
+
+/* Statistics of the last perft launch: subtree tasks, tasks taken from
+ * another block's range, interior nodes generated, leaf-parent nodes
+ * bulk-counted, device time of the work-stealing kernel (ms). */
+typedef struct {
+  uint64_t tasks;
+  uint64_t steals;
+  uint64_t interior_nodes;
+  uint64_t counted_nodes;
+  float kernel_ms;
+  float total_ms;
+} zeta_perft_stats;
+int zeta_perft_last_stats(zeta_perft_stats *st);
+
+/* ------------------------------------------------------------------ */
+/* Seeded synthetic positions generated on the device (the benchmark
+ * workloads): position i is a pure function of (seed, i), see
+ * zeta_gb300/csrc/positions.cu.  Host buffers: boards n*7, stm n,
+ * depth n.  Returns ZETA_ERR_DEVICE if some position found no playout
+ * meeting the constraints after 64 attempts (its depth is set to 0). */
+int zeta_make_positions(uint64_t seed, int n, int min_plies, int max_plies, int min_pieces, int min_depth,
+                        int max_depth, uint64_t *boards, uint8_t *stm, uint8_t *depth);
+
+/* Measured 32-bit integer-ALU throughput of the device in Tops/s (lop3 and
+ * shf instructions on every SM): the roofline denominator of the perft and
+ * search kernels. */
+int zeta_int_peak(double *tops);
+
+/* ------------------------------------------------------------------ */
+/* Move generation on the device (test and tooling entry): legal moves of
+ * n positions, max 256 each, in the reference packing; counts[i] moves
+ * for board i.  qs != 0 keeps captures only.  Host buffers. */
+int zeta_genmoves_batch(const uint64_t *boards, const uint8_t *stm, int n, int qs, uint32_t *moves,
+                        int32_t *counts);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

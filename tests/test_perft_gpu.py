@@ -1,0 +1,146 @@
+"""Perft on the GB300 through the C ABI, checked against the reference's
+known answers, the reference kernels' own counts (golden fixtures) and the
+oracle.  Integer work: every comparison is bit-exact."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import oracle_lib as ol
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def load(name):
+    return json.load(open(os.path.join(GOLD, name)))
+
+
+def board_of(case):
+    return np.array([int(x, 16) for x in case["board"]], dtype=np.uint64)
+
+
+def test_selftest_kats(zeta_device):
+    """src/test.c:43-73, one call per KAT as selftest() does."""
+    z = zeta_device
+    for case in load("perft_kat.json"):
+        b, stm = ol.setboard(case["fen"])
+        assert z.perft(b, stm, case["depth"]) == case["leaves"], case
+
+
+def test_reference_kernel_counts_batched(zeta_device):
+    """Every fixture made by the unmodified reference kernel, in one batch."""
+    z = zeta_device
+    cases = load("perft_ref.json")
+    boards = np.stack([board_of(c) for c in cases])
+    stm = np.array([c["stm"] for c in cases], dtype=np.uint8)
+    depth = np.array([c["depth"] for c in cases], dtype=np.uint8)
+    got = z.perft_batch(boards, stm, depth)
+    want = np.array([c["leaves"] for c in cases], dtype=np.uint64)
+    bad = [(cases[i]["name"], int(got[i]), int(want[i])) for i in np.nonzero(got != want)[0]]
+    assert not bad, bad[:10]
+
+
+def test_startpos_depth6(zeta_device):
+    """Depth 6 of the initial position: the headline single-position case."""
+    z = zeta_device
+    b, s = ol.setboard("rnbqkbnr/pppppppp/8/8/8/8/PPPPPPPP/RNBQKBNR w KQkq - 0 1")
+    assert z.perft(b, s, 6) == 119060324
+
+
+def test_random_positions_vs_oracle(zeta_device):
+    z = zeta_device
+    boards, stm, depth = ol.make_positions(0xBEEF, 200, min_plies=1, max_plies=150, min_depth=1, max_depth=3)
+    got = z.perft_batch(boards, stm, depth)
+    want = np.array([ol.perft(boards[i], stm[i], depth[i]) for i in range(len(depth))], dtype=np.uint64)
+    assert np.array_equal(got, want)
+
+
+def test_edge_depths_and_terminal_positions(zeta_device):
+    z = zeta_device
+    b, s = ol.setboard("rnbqkbnr/pppppppp/8/8/8/8/PPPPPPPP/RNBQKBNR w KQkq - 0 1")
+    assert z.perft(b, s, 0) == 1
+    assert z.perft(b, s, 1) == 20
+    mate, ms = ol.setboard("rnb1kbnr/pppp1ppp/8/4p3/6Pq/5P2/PPPPP2P/RNBQKBNR w KQkq - 1 3")
+    stale, ss = ol.setboard("7k/5Q2/6K1/8/8/8/8/8 b - - 0 1")
+    for d in (1, 2, 3):
+        assert z.perft(mate, ms, d) == 0
+        assert z.perft(stale, ss, d) == 0
+    assert z.perft(mate, ms, 0) == 1
+
+
+def test_bad_arguments_are_rejected(zeta_device):
+    z = zeta_device
+    b = np.array(z.STARTPOS)
+    with pytest.raises(z.ZetaError):
+        z.perft(b, 0, 99)
+    with pytest.raises(ValueError):
+        z.perft_batch(np.stack([b, b]), np.zeros(1, np.uint8), np.ones(2, np.uint8))
+
+
+def test_launch_shapes_do_not_change_counts(zeta_device):
+    """Block size, split policy and graph replay are scheduling only."""
+    z = zeta_device
+    boards, stm, depth = ol.make_positions(0xC0FFEE, 64, min_plies=10, max_plies=60, min_depth=2, max_depth=4)
+    base = z.perft_batch(boards, stm, depth)
+    saved = z.perft_config()
+    try:
+        for tpb in (64, 128, 256, 512):
+            for td in (1, 2, 3):
+                for mt in (0, 1000, 10**7):
+                    for graph in (True, False):
+                        z.perft_configure(threads_per_block=tpb, task_depth=td, min_tasks=mt, use_graph=graph)
+                        assert np.array_equal(z.perft_batch(boards, stm, depth), base), (tpb, td, mt, graph)
+    finally:
+        z.perft_configure(**saved)
+
+
+def test_graph_replay_is_repeatable(zeta_device):
+    z = zeta_device
+    boards, stm, depth = ol.make_positions(0xFACE, 300, min_plies=10, max_plies=60, min_depth=3, max_depth=4)
+    first = z.perft_batch(boards, stm, depth)
+    for _ in range(3):
+        assert np.array_equal(z.perft_batch(boards, stm, depth), first)
+    st = z.perft_stats()
+    assert st["tasks"] > 0 and st["counted_nodes"] > 0
+
+
+def test_batch_workload_sample_vs_reference_sum_of_children(zeta_device):
+    """Size-independent check at the benchmark's depths: a position's count
+    equals the sum of its children's counts one ply shallower."""
+    z = zeta_device
+    w = dict(z.WORKLOADS["perft_batch"])
+    boards, stm, depth = z.make_positions(w["seed"], 24, w["min_plies"], w["max_plies"], w["min_pieces"],
+                                          w["min_depth"], w["max_depth"])
+    whole = z.perft_batch(boards, stm, depth)
+    for i in range(len(depth)):
+        kids = [ol.play(boards[i], stm[i], m, perft_flags=True) for m in ol.genmoves(boards[i], stm[i])]
+        if not kids:
+            assert whole[i] == 0
+            continue
+        sub = z.perft_batch(np.stack(kids), np.full(len(kids), 1 - stm[i], np.uint8),
+                            np.full(len(kids), depth[i] - 1, np.uint8))
+        assert int(sub.sum()) == int(whole[i])
+
+
+def test_genmoves_matches_oracle(zeta_device):
+    z = zeta_device
+    boards, stm, _ = ol.make_positions(0xD00D, 400, min_plies=1, max_plies=200)
+    for qs in (False, True):
+        lists = z.genmoves_batch(boards, stm, qs=qs)
+        for i in range(len(stm)):
+            assert sorted(lists[i].tolist()) == sorted(ol.genmoves(boards[i], stm[i], qs)), i
+
+
+def test_device_positions_match_oracle_generator(zeta_device):
+    z = zeta_device
+    for name in ("perft_batch", "search_batch"):
+        w = dict(z.WORKLOADS[name])
+        n = 64
+        gb, gs, gd = z.make_positions(w["seed"], n, w["min_plies"], w["max_plies"], w["min_pieces"],
+                                      w["min_depth"], w["max_depth"])
+        ob, os_, od = ol.make_positions(w["seed"], n, min_plies=w["min_plies"], max_plies=w["max_plies"],
+                                        min_pieces=w["min_pieces"], min_depth=w["min_depth"],
+                                        max_depth=w["max_depth"])
+        assert np.array_equal(gb, ob) and np.array_equal(gs, os_) and np.array_equal(gd, od), name

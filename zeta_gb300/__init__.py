@@ -1,0 +1,220 @@
+"""zeta_gb300 -- GB300-native device path of the Zeta chess engine.
+
+Python binding of ``libzeta_cuda.so`` (C ABI in ``include/zeta_cuda.h``).
+The library is built in-tree by ``zeta_gb300.build`` (``__graft_entry__.build()``);
+importing this module does not build anything, and every call fails loudly
+when the library or a GB300 is missing -- there is no CPU fallback.
+
+Boards are the reference quad-bitboard (7 x u64, src/types.h:59-66) as numpy
+``uint64`` arrays of shape (7,) or (n, 7).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from typing import Optional
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libzeta_cuda.so")
+ROOT = os.path.dirname(_HERE)
+
+ZETA_OK = 0
+ERROR_NAMES = {
+    -1: "ZETA_ERR_CUDA",
+    -2: "ZETA_ERR_ARG",
+    -3: "ZETA_ERR_STATE",
+    -4: "ZETA_ERR_CAPACITY",
+    -5: "ZETA_ERR_DEVICE",
+    -6: "ZETA_ERR_BUDGET",
+    -7: "ZETA_ERR_NOALLOC",
+}
+
+
+class ZetaError(RuntimeError):
+    def __init__(self, code: int, message: str):
+        super().__init__(f"{ERROR_NAMES.get(code, code)}: {message}")
+        self.code = code
+
+
+class PerftConfig(ctypes.Structure):
+    _fields_ = [
+        ("threads_per_block", ctypes.c_int),
+        ("blocks_per_sm", ctypes.c_int),
+        ("min_tasks", ctypes.c_uint32),
+        ("task_depth", ctypes.c_int),
+        ("use_graph", ctypes.c_int),
+    ]
+
+
+class PerftStats(ctypes.Structure):
+    _fields_ = [
+        ("tasks", ctypes.c_uint64),
+        ("steals", ctypes.c_uint64),
+        ("interior_nodes", ctypes.c_uint64),
+        ("counted_nodes", ctypes.c_uint64),
+        ("kernel_ms", ctypes.c_float),
+        ("total_ms", ctypes.c_float),
+    ]
+
+
+_u64p = ctypes.POINTER(ctypes.c_uint64)
+_u8p = ctypes.POINTER(ctypes.c_uint8)
+_u32p = ctypes.POINTER(ctypes.c_uint32)
+_i32p = ctypes.POINTER(ctypes.c_int32)
+
+# every symbol include/zeta_cuda.h declares, with its ctypes signature
+SIGNATURES = {
+    "zeta_init": (ctypes.c_int, [ctypes.c_int, ctypes.c_uint64, ctypes.c_uint64]),
+    "zeta_release": (ctypes.c_int, []),
+    "zeta_last_error": (ctypes.c_char_p, []),
+    "zeta_device_info": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                                        ctypes.POINTER(ctypes.c_int), _u64p]),
+    "zeta_perft": (ctypes.c_int, [_u64p, ctypes.c_int, ctypes.c_int, _u64p]),
+    "zeta_perft_batch": (ctypes.c_int, [_u64p, _u8p, _u8p, ctypes.c_int, _u64p]),
+    "zeta_perft_batch_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                               ctypes.c_void_p, ctypes.c_void_p]),
+    "zeta_perft_configure": (ctypes.c_int, [ctypes.POINTER(PerftConfig)]),
+    "zeta_perft_get_config": (ctypes.c_int, [ctypes.POINTER(PerftConfig)]),
+    "zeta_perft_last_stats": (ctypes.c_int, [ctypes.POINTER(PerftStats)]),
+    "zeta_make_positions": (ctypes.c_int, [ctypes.c_uint64, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                           ctypes.c_int, ctypes.c_int, _u64p, _u8p, _u8p]),
+    "zeta_int_peak": (ctypes.c_int, [ctypes.POINTER(ctypes.c_double)]),
+    "zeta_genmoves_batch": (ctypes.c_int, [_u64p, _u8p, ctypes.c_int, ctypes.c_int, _u32p, _i32p]),
+}
+
+_lib: Optional[ctypes.CDLL] = None
+
+
+def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
+    """Load libzeta_cuda.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise ZetaError(-3, f"{path} is missing: run __graft_entry__.build() (nvcc, sm_103a)")
+    lib = ctypes.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def _check(rc: int) -> None:
+    if rc != ZETA_OK:
+        msg = load_library().zeta_last_error().decode(errors="replace")
+        raise ZetaError(rc, msg)
+
+
+def _ptr(a: np.ndarray, t):
+    return a.ctypes.data_as(t)
+
+
+# ---------------------------------------------------------------- lifecycle
+def init(device: int = 0, tt1_mb: int = 0, tt2_mb: int = 0) -> None:
+    _check(load_library().zeta_init(device, tt1_mb, tt2_mb))
+
+
+def release() -> None:
+    _check(load_library().zeta_release())
+
+
+def device_info() -> dict:
+    sms, ma, mi = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    hbm = ctypes.c_uint64()
+    _check(load_library().zeta_device_info(ctypes.byref(sms), ctypes.byref(ma), ctypes.byref(mi), ctypes.byref(hbm)))
+    return {"sms": sms.value, "cc": (ma.value, mi.value), "hbm_bytes": hbm.value}
+
+
+# ---------------------------------------------------------------- perft
+def perft(board: np.ndarray, stm: int, depth: int) -> int:
+    b = np.ascontiguousarray(board, dtype=np.uint64).reshape(7)
+    out = ctypes.c_uint64()
+    _check(load_library().zeta_perft(_ptr(b, _u64p), int(stm), int(depth), ctypes.byref(out)))
+    return out.value
+
+
+def perft_batch(boards: np.ndarray, stm: np.ndarray, depth: np.ndarray) -> np.ndarray:
+    b = np.ascontiguousarray(boards, dtype=np.uint64).reshape(-1, 7)
+    s = np.ascontiguousarray(stm, dtype=np.uint8)
+    d = np.ascontiguousarray(depth, dtype=np.uint8)
+    n = b.shape[0]
+    if s.shape != (n,) or d.shape != (n,):
+        raise ValueError("stm and depth need one entry per board")
+    out = np.zeros(n, dtype=np.uint64)
+    _check(load_library().zeta_perft_batch(_ptr(b, _u64p), _ptr(s, _u8p), _ptr(d, _u8p), n, _ptr(out, _u64p)))
+    return out
+
+
+def perft_batch_device(d_boards: int, d_stm: int, d_depth: int, n: int, d_leaves: int, stream: int = 0) -> None:
+    """Device pointers (e.g. torch ``data_ptr()``); ``stream`` a cudaStream_t handle."""
+    _check(load_library().zeta_perft_batch_device(d_boards, d_stm, d_depth, n, d_leaves, stream))
+
+
+def perft_configure(threads_per_block: int = 128, blocks_per_sm: int = 0, min_tasks: int = 0, task_depth: int = 3,
+                    use_graph: bool = True) -> None:
+    cfg = PerftConfig(threads_per_block, blocks_per_sm, min_tasks, task_depth, int(use_graph))
+    _check(load_library().zeta_perft_configure(ctypes.byref(cfg)))
+
+
+def perft_config() -> dict:
+    cfg = PerftConfig()
+    _check(load_library().zeta_perft_get_config(ctypes.byref(cfg)))
+    return {f: getattr(cfg, f) for f, _ in PerftConfig._fields_}
+
+
+def perft_stats() -> dict:
+    st = PerftStats()
+    _check(load_library().zeta_perft_last_stats(ctypes.byref(st)))
+    return {f: getattr(st, f) for f, _ in PerftStats._fields_}
+
+
+# ---------------------------------------------------------------- positions / movegen
+def make_positions(seed: int, n: int, min_plies: int, max_plies: int, min_pieces: int = 0, min_depth: int = 0,
+                   max_depth: int = 0):
+    boards = np.zeros((n, 7), dtype=np.uint64)
+    stm = np.zeros(n, dtype=np.uint8)
+    depth = np.zeros(n, dtype=np.uint8)
+    _check(load_library().zeta_make_positions(seed & (2**64 - 1), n, min_plies, max_plies, min_pieces, min_depth,
+                                              max_depth, _ptr(boards, _u64p), _ptr(stm, _u8p), _ptr(depth, _u8p)))
+    return boards, stm, depth
+
+
+def int_peak_tops() -> float:
+    """Measured int32 ALU throughput (Tops/s) of the initialised device."""
+    t = ctypes.c_double()
+    _check(load_library().zeta_int_peak(ctypes.byref(t)))
+    return t.value
+
+
+def genmoves_batch(boards: np.ndarray, stm: np.ndarray, qs: bool = False):
+    b = np.ascontiguousarray(boards, dtype=np.uint64).reshape(-1, 7)
+    s = np.ascontiguousarray(stm, dtype=np.uint8)
+    n = b.shape[0]
+    moves = np.zeros((n, 256), dtype=np.uint32)
+    counts = np.zeros(n, dtype=np.int32)
+    _check(load_library().zeta_genmoves_batch(_ptr(b, _u64p), _ptr(s, _u8p), n, int(qs), _ptr(moves, _u32p),
+                                              _ptr(counts, _i32p)))
+    return [moves[i, : counts[i]].copy() for i in range(n)]
+
+
+# workload definitions of the benchmark configurations (seeded, synthetic)
+SEED_BASE = 0x5A17A0000000001
+WORKLOADS = {
+    # batched perft: 4096 playouts of 10-60 plies, depth 3-5
+    "perft_batch": dict(seed=SEED_BASE + 2, n=4096, min_plies=10, max_plies=60, min_pieces=0, min_depth=3,
+                        max_depth=5),
+    # batched search: 1024 playouts of 20-40 plies with >= 20 pieces
+    "search_batch": dict(seed=SEED_BASE + 3, n=1024, min_plies=20, max_plies=40, min_pieces=20, min_depth=7,
+                         max_depth=7),
+    # full engine: 256 playouts of 20-40 plies with >= 20 pieces
+    "engine": dict(seed=SEED_BASE + 5, n=256, min_plies=20, max_plies=40, min_pieces=20, min_depth=12,
+                   max_depth=12),
+}
+
+# the initial position as setboard leaves it (src/io.c:335-531), white to move
+STARTPOS = np.array([0xFFFF000000000000, 0x91FF00000000FF91, 0x5A0000000000005A, 0xAD000000000000AD,
+                     0x6EFFFFFFFFFFFF6E, 0x18892007F9451009, 0], dtype=np.uint64)

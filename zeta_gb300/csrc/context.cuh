@@ -1,0 +1,103 @@
+/*
+ * context.cuh -- device state of libzeta_cuda.so (internal).
+ *
+ * One context per process, as the reference keeps one OpenCL context in
+ * globals (src/zeta.c:56-139).  It owns the stream, the perft work
+ * arena, the transposition tables and the staging buffers of the
+ * host-buffer entry points.
+ */
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/zeta_cuda.h"
+#include "chess.cuh"
+
+namespace zeta {
+
+/* One subtree of a perft launch: a position, its side to move, its
+ * remaining depth and the batch index whose count it adds to. 48 bytes. */
+struct __align__(16) Task {
+  Pos pos;
+  uint32_t root;
+  uint8_t stm;
+  uint8_t depth;
+  uint16_t pad;
+};
+
+constexpr int kMaxLevels = 12;   /* split levels per launch: depth <= 15 */
+constexpr int kMaxDepth = 15;
+
+/* device-side counters of one perft launch */
+struct PerftCounters {
+  uint32_t level_n[kMaxLevels + 1]; /* nodes per split level */
+  uint32_t n_final;                 /* subtree tasks */
+  uint32_t status;                  /* ZETA_ERR_* as positive bits, 0 = fine */
+  uint32_t pad;
+  unsigned long long steals;
+  unsigned long long interior;
+  unsigned long long counted;
+};
+
+struct Context {
+  bool ready = false;
+  int device = 0;
+  int sms = 0;
+  int cc_major = 0, cc_minor = 0;
+  size_t hbm = 0;
+  cudaStream_t stream = nullptr;
+
+  /* perft arena */
+  Task *lvl[2] = {nullptr, nullptr};
+  Task *fin = nullptr;
+  uint32_t cap_lvl = 0, cap_fin = 0;
+  PerftCounters *pc = nullptr;
+  uint32_t *cursors = nullptr;
+  int cursors_cap = 0;
+
+  /* staging for host-buffer calls */
+  uint64_t *d_boards = nullptr;
+  uint8_t *d_stm = nullptr, *d_depth = nullptr;
+  uint64_t *d_leaves = nullptr;
+  int stage_cap = 0;
+  void *h_pinned = nullptr;
+  size_t h_pinned_bytes = 0;
+
+  zeta_perft_config pcfg{128, 0, 0, 3, 1};
+  zeta_perft_stats pstats{};
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+
+  /* cached CUDA graph of the last perft launch sequence */
+  cudaGraphExec_t graph = nullptr;
+  const void *g_boards = nullptr, *g_stm = nullptr, *g_depth = nullptr, *g_leaves = nullptr;
+  int g_n = -1;
+  cudaStream_t g_stream = nullptr;
+  zeta_perft_config g_cfg{};
+
+  /* transposition tables (search) */
+  void *tt1 = nullptr, *tt2 = nullptr;
+  uint64_t tt1_entries = 0, tt2_entries = 0;
+};
+
+Context &ctx();
+int set_error(int code, const char *fmt, ...);
+int cuda_fail(cudaError_t e, const char *what);
+
+#define ZCHECK(call)                                   \
+  do {                                                 \
+    cudaError_t _e = (call);                           \
+    if (_e != cudaSuccess) return cuda_fail(_e, #call); \
+  } while (0)
+
+/* perft.cu */
+int perft_launch(const uint64_t *d_boards, const uint8_t *d_stm, const uint8_t *d_depth, int n,
+                 uint64_t *d_leaves, cudaStream_t stream);
+int perft_ensure_arena(uint64_t tasks_cap);
+int positions_launch(u64 seed, int n, int min_plies, int max_plies, int min_pieces, int min_depth, int max_depth,
+                     uint64_t *d_boards, uint8_t *d_stm, uint8_t *d_depth, uint32_t *d_fail, cudaStream_t s);
+int int_peak(double *tops);
+int genmoves_launch(const uint64_t *d_boards, const uint8_t *d_stm, int n, int qs, uint32_t *d_moves,
+                    int32_t *d_counts, cudaStream_t stream);
+
+}  // namespace zeta
