@@ -147,7 +147,9 @@ def run_ours(args):
     d_depth = torch.from_numpy(depth).to(dev)
     d_leaves = torch.zeros(n, dtype=torch.int64, device=dev)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device=dev)
-    stream = torch.cuda.current_stream(dev)
+    # a non-default stream: the library captures its launch sequence on it
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
     sp = stream.cuda_stream
 
     def step():

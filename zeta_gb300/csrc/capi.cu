@@ -94,6 +94,7 @@ int zeta_init(int device, uint64_t tt1_mb, uint64_t tt2_mb) {
   c.hbm = prop.totalGlobalMem;
   ZCHECK(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
   for (int i = 0; i < 4; i++) ZCHECK(cudaEventCreate(&c.ev[i]));
+  for (int i = 0; i < 2; i++) ZCHECK(cudaEventCreateWithFlags(&c.ev_join[i], cudaEventDisableTiming));
   ZCHECK(cudaMalloc(&c.pc, sizeof(PerftCounters)));
   /* transposition tables, zeroed as cl_init_device does from the host
    * zero images (clrun.c:404-443) */
@@ -129,6 +130,8 @@ int zeta_release(void) {
   cudaFree(c.tt2);
   for (int i = 0; i < 4; i++)
     if (c.ev[i]) cudaEventDestroy(c.ev[i]);
+  for (int i = 0; i < 2; i++)
+    if (c.ev_join[i]) cudaEventDestroy(c.ev_join[i]);
   if (c.stream) cudaStreamDestroy(c.stream);
   c = Context();
   return ZETA_OK;

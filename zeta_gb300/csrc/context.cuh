@@ -67,6 +67,7 @@ struct Context {
   zeta_perft_config pcfg{128, 0, 0, 3, 1};
   zeta_perft_stats pstats{};
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  cudaEvent_t ev_join[2] = {nullptr, nullptr}; /* ordering with a caller's stream */
 
   /* cached CUDA graph of the last perft launch sequence */
   cudaGraphExec_t graph = nullptr;

@@ -276,6 +276,9 @@ int perft_ensure_arena(uint64_t tasks_cap) {
   return ZETA_OK;
 }
 
+int perft_run(const uint64_t *d_boards, const uint8_t *d_stm, const uint8_t *d_depth, int n, uint64_t *d_leaves,
+              cudaStream_t s);
+
 static int ws_geometry(int &blocks, int &tpb) {
   Context &c = ctx();
   tpb = c.pcfg.threads_per_block;
@@ -302,7 +305,7 @@ static int ws_geometry(int &blocks, int &tpb) {
 
 /* enqueue the whole launch sequence on `s` */
 static int perft_enqueue(const uint64_t *d_boards, const uint8_t *d_stm, const uint8_t *d_depth, int n,
-                         uint64_t *d_leaves, cudaStream_t s, int blocks, int tpb, bool timed) {
+                         uint64_t *d_leaves, cudaStream_t s, int blocks, int tpb, bool timed, bool capturing) {
   Context &c = ctx();
   uint32_t min_tasks = c.pcfg.min_tasks ? c.pcfg.min_tasks : (uint32_t)(4ull * blocks * tpb);
   ZCHECK(cudaMemsetAsync(c.pc, 0, sizeof(PerftCounters), s));
@@ -314,17 +317,40 @@ static int perft_enqueue(const uint64_t *d_boards, const uint8_t *d_stm, const u
                                       min_tasks, c.pcfg.task_depth, c.pc);
     ZCHECK(cudaGetLastError());
   }
-  if (timed) ZCHECK(cudaEventRecord(c.ev[1], s));
+  /* external records: inside a stream capture they become event-record
+   * nodes of the graph, so the kernel can be timed on every replay */
+  if (timed) ZCHECK(capturing ? cudaEventRecordWithFlags(c.ev[1], s, cudaEventRecordExternal) : cudaEventRecord(c.ev[1], s));
   ws_kernel(tpb)<<<blocks, tpb, 0, s>>>(c.fin, c.cursors, d_leaves, c.pc);
   ZCHECK(cudaGetLastError());
-  if (timed) ZCHECK(cudaEventRecord(c.ev[2], s));
+  if (timed) ZCHECK(capturing ? cudaEventRecordWithFlags(c.ev[2], s, cudaEventRecordExternal) : cudaEventRecord(c.ev[2], s));
   return ZETA_OK;
 }
 
 int perft_launch(const uint64_t *d_boards, const uint8_t *d_stm, const uint8_t *d_depth, int n, uint64_t *d_leaves,
-                 cudaStream_t s) {
+                 cudaStream_t user) {
   Context &c = ctx();
   if (n <= 0) return set_error(ZETA_ERR_ARG, "batch size must be positive");
+  /* the legacy default stream cannot be captured: run on the library's
+   * stream, ordered after the caller's work and before its next work */
+  cudaStream_t s = user;
+  bool joined = false;
+  if (user == nullptr || user == cudaStreamLegacy || user == cudaStreamPerThread) {
+    s = c.stream;
+    joined = true;
+    ZCHECK(cudaEventRecord(c.ev_join[0], user));
+    ZCHECK(cudaStreamWaitEvent(s, c.ev_join[0], 0));
+  }
+  int rc = perft_run(d_boards, d_stm, d_depth, n, d_leaves, s);
+  if (joined) {
+    ZCHECK(cudaEventRecord(c.ev_join[1], s));
+    ZCHECK(cudaStreamWaitEvent(user, c.ev_join[1], 0));
+  }
+  return rc;
+}
+
+int perft_run(const uint64_t *d_boards, const uint8_t *d_stm, const uint8_t *d_depth, int n, uint64_t *d_leaves,
+              cudaStream_t s) {
+  Context &c = ctx();
   if (c.pcfg.task_depth < 1 || c.pcfg.task_depth > 3) return set_error(ZETA_ERR_ARG, "task_depth must be 1..3");
   int blocks, tpb;
   int rc = ws_geometry(blocks, tpb);
@@ -347,7 +373,7 @@ int perft_launch(const uint64_t *d_boards, const uint8_t *d_stm, const uint8_t *
       }
       cudaGraph_t g;
       ZCHECK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-      rc = perft_enqueue(d_boards, d_stm, d_depth, n, d_leaves, s, blocks, tpb, true);
+      rc = perft_enqueue(d_boards, d_stm, d_depth, n, d_leaves, s, blocks, tpb, true, true);
       cudaError_t e = cudaStreamEndCapture(s, &g);
       if (rc) return rc;
       if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
@@ -364,7 +390,7 @@ int perft_launch(const uint64_t *d_boards, const uint8_t *d_stm, const uint8_t *
     }
     ZCHECK(cudaGraphLaunch(c.graph, s));
   } else {
-    rc = perft_enqueue(d_boards, d_stm, d_depth, n, d_leaves, s, blocks, tpb, true);
+    rc = perft_enqueue(d_boards, d_stm, d_depth, n, d_leaves, s, blocks, tpb, true, false);
     if (rc) return rc;
   }
   ZCHECK(cudaEventRecord(c.ev[3], s));
@@ -375,8 +401,9 @@ int perft_launch(const uint64_t *d_boards, const uint8_t *d_stm, const uint8_t *
   c.pstats.steals = h.steals;
   c.pstats.interior_nodes = h.interior;
   c.pstats.counted_nodes = h.counted;
-  cudaEventElapsedTime(&c.pstats.kernel_ms, c.ev[1], c.ev[2]);
-  cudaEventElapsedTime(&c.pstats.total_ms, c.ev[0], c.ev[3]);
+  if (cudaEventElapsedTime(&c.pstats.kernel_ms, c.ev[1], c.ev[2]) != cudaSuccess) c.pstats.kernel_ms = -1.f;
+  if (cudaEventElapsedTime(&c.pstats.total_ms, c.ev[0], c.ev[3]) != cudaSuccess) c.pstats.total_ms = -1.f;
+  (void)cudaGetLastError(); /* a failed timing query must not poison the next call */
   if (h.status & ST_CAPACITY) {
     /* grow the arena for the next call and report */
     uint64_t need = std::max<uint64_t>(h.n_final, 0);
