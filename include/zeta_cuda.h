@@ -66,6 +66,25 @@ int zeta_perft_batch(const uint64_t *boards, const uint8_t *stm, const uint8_t *
 int zeta_perft_batch_device(const uint64_t *d_boards, const uint8_t *d_stm, const uint8_t *d_depth,
                             int n, uint64_t *d_leaves, void *stream);
 
+/* Same work as zeta_perft_batch_device for callers that cannot allocate
+ * device memory: programs that own every byte of device memory through
+ * their own pool or budget, and latency-critical loops where a cudaMalloc
+ * (which may synchronise the device) is not allowed.  No counterpart in
+ * the reference.  It calls no cudaMalloc/cudaFree and needs no zeta_init:
+ * its scratch is one fixed device array of about 19 MB inside the library,
+ * held by every GPU that loads it until the process exits.
+ *  - Limits: n <= 131072 positions, and the tree split may make at most
+ *    131072 subtree tasks per level; beyond either it returns
+ *    ZETA_ERR_NOALLOC.
+ *  - The first call on a device looks up the array's device address (its
+ *    host-side name is not a device address); make that first call before
+ *    any stream capture.
+ *  - All calls share the one array: calls that overlap on the GPU (other
+ *    streams, other host threads) race and give wrong counts.  The call
+ *    synchronises `stream` before returning. */
+int zeta_perft_batch_noalloc(const uint64_t *d_boards, const uint8_t *d_stm, const uint8_t *d_depth, int n,
+                             uint64_t *d_leaves, void *stream);
+
 /* Launch geometry and split policy of the perft path (autotuner knobs).
  * threads_per_block: 64..1024, multiple of 32; blocks_per_sm: 0 = from
  * occupancy; min_tasks: split the tree until at least this many subtree

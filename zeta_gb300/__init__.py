@@ -75,6 +75,8 @@ SIGNATURES = {
     "zeta_perft_batch": (ctypes.c_int, [_u64p, _u8p, _u8p, ctypes.c_int, _u64p]),
     "zeta_perft_batch_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
                                                ctypes.c_void_p, ctypes.c_void_p]),
+    "zeta_perft_batch_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                                ctypes.c_void_p, ctypes.c_void_p]),
     "zeta_perft_configure": (ctypes.c_int, [ctypes.POINTER(PerftConfig)]),
     "zeta_perft_get_config": (ctypes.c_int, [ctypes.POINTER(PerftConfig)]),
     "zeta_perft_last_stats": (ctypes.c_int, [ctypes.POINTER(PerftStats)]),

@@ -424,4 +424,88 @@ int genmoves_launch(const uint64_t *d_boards, const uint8_t *d_stm, int n, int q
   return ZETA_OK;
 }
 
+/* ------------------------------------------------------------------ */
+/* Batched perft for callers that cannot allocate device memory.
+ *
+ * Some programs that embed the engine own every byte of device memory
+ * themselves (a host application with a fixed memory budget and its own
+ * pool), or run a latency-critical loop in which a cudaMalloc -- which
+ * may synchronise the whole device -- is not acceptable.  For them,
+ * zeta_perft_batch_noalloc runs the same launch sequence as
+ * zeta_perft_batch_device with all of its scratch (task arrays, counters,
+ * work-stealing cursors) in one fixed file-scope device array instead of
+ * buffers allocated by the library.  The caller passes the inputs and
+ * outputs, already in device memory. */
+namespace {
+constexpr uint32_t kNoAllocMaxTasks = 1u << 17; /* per task array: 131072 subtrees */
+constexpr int kNoAllocMaxBlocks = 4096;         /* work-stealing cursors */
+
+struct NoAllocScratch {
+  PerftCounters pc;
+  uint32_t cursors[kNoAllocMaxBlocks];
+  Task lvl[2][kNoAllocMaxTasks];
+  Task fin[kNoAllocMaxTasks];
+};
+
+/* about 19 MB; every GPU that loads the library holds it until exit */
+static __device__ __align__(256) unsigned char g_noalloc_scratch[sizeof(NoAllocScratch)];
+
+constexpr int kNoAllocMaxDevices = 64;
+NoAllocScratch *g_noalloc_ptr[kNoAllocMaxDevices] = {nullptr};
+int g_noalloc_sms[kNoAllocMaxDevices] = {0};
+int g_noalloc_blocks[kNoAllocMaxDevices] = {0};
+}  // namespace
+
 }  // namespace zeta
+
+using namespace zeta;
+
+extern "C" int zeta_perft_batch_noalloc(const uint64_t *d_boards, const uint8_t *d_stm, const uint8_t *d_depth,
+                                        int n, uint64_t *d_leaves, void *stream) {
+  if (!d_boards || !d_stm || !d_depth || !d_leaves) return set_error(ZETA_ERR_ARG, "null buffer");
+  if (n <= 0 || (uint32_t)n > kNoAllocMaxTasks)
+    return set_error(ZETA_ERR_NOALLOC, "batch of %d positions outside 1..%u (fixed scratch)", n, kNoAllocMaxTasks);
+  int dev = 0;
+  ZCHECK(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kNoAllocMaxDevices) return set_error(ZETA_ERR_ARG, "device %d out of range", dev);
+  /* set-up, once per device, with that device current: the host-side name
+   * of the array is not a device address, so look the address up */
+  if (!g_noalloc_ptr[dev]) {
+    void *p = nullptr;
+    ZCHECK(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+    int sms = 0, bps = 0;
+    ZCHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    ZCHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_perft_ws<128>, 128, 0));
+    int blocks = sms * (bps > 0 ? bps : 1);
+    if (blocks > kNoAllocMaxBlocks) blocks = kNoAllocMaxBlocks;
+    g_noalloc_sms[dev] = sms;
+    g_noalloc_blocks[dev] = blocks;
+    g_noalloc_ptr[dev] = (NoAllocScratch *)p;
+  }
+  NoAllocScratch *S = g_noalloc_ptr[dev];
+  const int blocks = g_noalloc_blocks[dev], sms = g_noalloc_sms[dev];
+  cudaStream_t s = (cudaStream_t)stream;
+  /* the array keeps the previous call's contents: clear what must start at zero */
+  ZCHECK(cudaMemsetAsync(&S->pc, 0, sizeof(PerftCounters), s));
+  ZCHECK(cudaMemsetAsync(S->cursors, 0, blocks * sizeof(uint32_t), s));
+  /* stop splitting early enough that the next level (about 35 children per
+   * node) still fits the fixed task arrays */
+  uint32_t min_tasks = (uint32_t)(4ull * blocks * 128);
+  if (min_tasks > kNoAllocMaxTasks / 64) min_tasks = kNoAllocMaxTasks / 64;
+  k_roots<<<(n + 127) / 128, 128, 0, s>>>(d_boards, d_stm, d_depth, n, S->lvl[0], d_leaves, &S->pc);
+  ZCHECK(cudaGetLastError());
+  for (int lv = 0; lv < kMaxLevels; lv++) {
+    k_split<<<sms * 4, 128, 0, s>>>(lv, S->lvl[lv & 1], S->lvl[(lv + 1) & 1], S->fin, kNoAllocMaxTasks,
+                                    kNoAllocMaxTasks, min_tasks, 3, &S->pc);
+    ZCHECK(cudaGetLastError());
+  }
+  k_perft_ws<128><<<blocks, 128, 0, s>>>(S->fin, S->cursors, d_leaves, &S->pc);
+  ZCHECK(cudaGetLastError());
+  uint32_t status = 0;
+  ZCHECK(cudaMemcpyAsync(&status, &S->pc.status, sizeof status, cudaMemcpyDeviceToHost, s));
+  ZCHECK(cudaStreamSynchronize(s));
+  if (status & ST_CAPACITY)
+    return set_error(ZETA_ERR_NOALLOC, "the split needs more than %u subtree tasks (fixed scratch)", kNoAllocMaxTasks);
+  if (status & ST_DEPTH) return set_error(ZETA_ERR_ARG, "perft depth above %d", kMaxDepth);
+  return ZETA_OK;
+}
