@@ -121,10 +121,10 @@ def measured_peaks():
     return {}
 
 
-def workload_arrays(z, rank: int):
+def workload_arrays(z, rank: int, n: int = 0):
     w = dict(z.WORKLOADS[WORKLOAD])
     seed = w["seed"] + 0x1000003 * rank  # each rank its own shard
-    return z.make_positions(seed, w["n"], w["min_plies"], w["max_plies"], w["min_pieces"], w["min_depth"],
+    return z.make_positions(seed, n or w["n"], w["min_plies"], w["max_plies"], w["min_pieces"], w["min_depth"],
                             w["max_depth"])
 
 
@@ -138,8 +138,10 @@ def run_ours(args):
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
     z.init(local, 0, 0)
+    from zeta_gb300.autotune import load_tuned
+    load_tuned(z)  # the autotuner's launch configuration, when recorded
     info = z.device_info()
-    boards, stm, depth = workload_arrays(z, rank)
+    boards, stm, depth = workload_arrays(z, rank, args.n)
     n = len(depth)
     dev = torch.device("cuda", local)
     d_boards = torch.from_numpy(boards.view(np.int64)).to(dev)
@@ -232,7 +234,7 @@ def run_ours(args):
                     "unit": "Tops/s", "frac": round(achieved / int_peak, 4), "traffic": traffic,
                     "peak_source": "measured: int32 LOP3/SHF/IADD3 microbenchmark (zeta_int_peak)",
                     "kernel": "k_perft_ws"}
-    cpu = cpu_baseline_sample(boards, stm, depth)
+    cpu = None if args.no_cpu else cpu_baseline_sample(boards, stm, depth)
     line = {
         "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(sum(step_ms) / len(step_ms), 4), "higher_is_better": True,
@@ -334,6 +336,8 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--n", type=int, default=0, help="positions per GPU (default: the workload's 4096)")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the timed CPU baseline (profiling runs)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -84,14 +84,20 @@ def test_launch_shapes_do_not_change_counts(zeta_device):
     z = zeta_device
     boards, stm, depth = ol.make_positions(0xC0FFEE, 64, min_plies=10, max_plies=60, min_depth=2, max_depth=4)
     base = z.perft_batch(boards, stm, depth)
+    from zeta_gb300.autotune import VARIANTS
     saved = z.perft_config()
     try:
-        for tpb in (64, 128, 256, 512):
-            for td in (1, 2, 3):
-                for mt in (0, 1000, 10**7):
-                    for graph in (True, False):
-                        z.perft_configure(threads_per_block=tpb, task_depth=td, min_tasks=mt, use_graph=graph)
-                        assert np.array_equal(z.perft_batch(boards, stm, depth), base), (tpb, td, mt, graph)
+        for tpb, bps in VARIANTS:
+            for td in (1, 2, 3, 4):
+                z.perft_configure(threads_per_block=tpb, blocks_per_sm=bps, task_depth=td)
+                assert np.array_equal(z.perft_batch(boards, stm, depth), base), (tpb, bps, td)
+        for mt in (0, 1000, 10**6):
+            for graph in (True, False):
+                z.perft_configure(threads_per_block=128, task_depth=3, min_tasks=mt, use_graph=graph)
+                assert np.array_equal(z.perft_batch(boards, stm, depth), base), (mt, graph)
+        with pytest.raises(z.ZetaError):
+            z.perft_configure(threads_per_block=128, blocks_per_sm=5, task_depth=3)
+            z.perft_batch(boards, stm, depth)
     finally:
         z.perft_configure(**saved)
 

@@ -114,6 +114,17 @@ def build_oracle(verbose: bool = False) -> None:
             print("reference kernels not built:", e, file=sys.stderr)
 
 
+def build_opcount(out: str | None = None) -> str:
+    """Compile and run the host op counter (csrc/opcount.cc): writes the
+    algorithmic int32 operations per perft node to profiles/opcount.json."""
+    os.makedirs(BUILD, exist_ok=True)
+    exe = os.path.join(BUILD, "opcount")
+    _run(["g++", "-O2", "-std=c++17", "-o", exe, os.path.join(CSRC, "opcount.cc")])
+    out = out or os.path.join(ROOT, "profiles", "opcount.json")
+    _run([exe, out])
+    return out
+
+
 def build_all(verbose: bool = False) -> None:
     build_cuda(verbose)
     build_host(verbose)

@@ -121,6 +121,7 @@ int zeta_release(void) {
   cudaFree(c.fin);
   cudaFree(c.pc);
   cudaFree(c.cursors);
+  cudaFree(c.scratch);
   cudaFree(c.d_boards);
   cudaFree(c.d_stm);
   cudaFree(c.d_depth);
@@ -149,7 +150,7 @@ int zeta_device_info(int *sm_count, int *cc_major, int *cc_minor, uint64_t *hbm_
 
 int zeta_perft_configure(const zeta_perft_config *cfg) {
   if (!cfg) return set_error(ZETA_ERR_ARG, "null config");
-  if (cfg->task_depth < 1 || cfg->task_depth > 3) return set_error(ZETA_ERR_ARG, "task_depth must be 1..3");
+  if (cfg->task_depth < 1 || cfg->task_depth > 4) return set_error(ZETA_ERR_ARG, "task_depth must be 1..4");
   int t = cfg->threads_per_block;
   if (t != 64 && t != 128 && t != 256 && t != 512)
     return set_error(ZETA_ERR_ARG, "threads_per_block must be 64, 128, 256 or 512");

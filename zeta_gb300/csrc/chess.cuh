@@ -27,9 +27,17 @@
 #define ZHD static inline
 #endif
 
+/* The bitboard word.  The op counter (opcount.cc) compiles this file on
+ * the host with a counting word type to measure the algorithmic integer
+ * operations per node; every other build uses plain 64-bit integers. */
+#ifndef ZETA_WORD_TYPE
+#define ZETA_WORD_TYPE unsigned long long
+#define ZETA_OPS(n) ((void)0)
+#endif
+
 namespace zeta {
 
-typedef unsigned long long u64;
+typedef ZETA_WORD_TYPE u64;
 typedef uint32_t Move;
 
 /* piece types and flag masks (src/types.h:94-124) */
@@ -57,21 +65,26 @@ struct Pos {
 };
 
 ZHD int popc(u64 x) {
+  ZETA_OPS(2);
 #if defined(__CUDA_ARCH__)
   return __popcll(x);
 #else
-  return __builtin_popcountll(x);
+  return __builtin_popcountll((unsigned long long)x);
 #endif
 }
 ZHD int ctz(u64 x) {
+  ZETA_OPS(2);
 #if defined(__CUDA_ARCH__)
   return __ffsll((long long)x) - 1;
 #else
-  return __builtin_ctzll(x);
+  return __builtin_ctzll((unsigned long long)x);
 #endif
 }
 /* OpenCL shift semantics: counts mod 64 */
-ZHD u64 bit(int sq) { return 1ULL << (sq & 63); }
+ZHD u64 bit(int sq) {
+  ZETA_OPS(4); /* a variable shift */
+  return u64(1ULL << (sq & 63));
+}
 
 /* The initial position as setboard leaves it (src/io.c:335-531): all
  * moved flags set except the six castle squares. */
@@ -89,8 +102,10 @@ ZHD Pos start_pos() {
 
 ZHD int piece_at(const Pos &p, int sq) {
   sq &= 63;
-  return (int)(((p.b0 >> sq) & 1) | (((p.p1 >> sq) & 1) << 1) | (((p.p2 >> sq) & 1) << 2) |
-               (((p.p3 >> sq) & 1) << 3));
+  ZETA_OPS(4 * 6 + 3 * 2); /* four variable shifts and masks, three ors */
+  const unsigned long long b0 = (unsigned long long)p.b0, p1 = (unsigned long long)p.p1,
+                           p2 = (unsigned long long)p.p2, p3 = (unsigned long long)p.p3;
+  return (int)(((b0 >> sq) & 1) | (((p1 >> sq) & 1) << 1) | (((p2 >> sq) & 1) << 2) | (((p3 >> sq) & 1) << 3));
 }
 
 /* ---------------- directions ----------------
@@ -231,7 +246,7 @@ ZHD Guard make_guard(const Sets &s, int stm) {
 
 /* Is `ksq` attacked after an en-passant capture?  post-move sets. */
 ZHD bool attacked_after(int ksq, u64 occ, u64 them, const Sets &s, int stm) {
-  u64 k = 1ULL << ksq;
+  u64 k = bit(ksq);
   u64 pro = ~occ;
   u64 erq = s.rq & them, ebq = s.bq & them;
   u64 a = ray_attacks<0>(k, pro) | ray_attacks<1>(k, pro) | ray_attacks<2>(k, pro) |
@@ -416,7 +431,7 @@ ZHD Move encode(const Pos &p, int stm, int from, int to) {
 template <int D>
 ZHD int slider_from(int to, u64 occ) {
   constexpr int R = (D & 1) ? D - 1 : D + 1; /* opposite direction */
-  u64 r = ray_attacks<R>(1ULL << to, ~occ);
+  u64 r = ray_attacks<R>(bit(to), ~occ);
   return ctz(r & occ);
 }
 

@@ -55,6 +55,8 @@ struct Context {
   PerftCounters *pc = nullptr;
   uint32_t *cursors = nullptr;
   int cursors_cap = 0;
+  Pos *scratch = nullptr;    /* per-block node buffers of the work-stealing kernel */
+  uint64_t scratch_cap = 0;  /* positions */
 
   /* staging for host-buffer calls */
   uint64_t *d_boards = nullptr;

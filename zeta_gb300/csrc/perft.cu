@@ -8,16 +8,21 @@
  *
  *   k_roots     batch -> level-0 tasks
  *   k_split     breadth-first split, one launch per level: a node becomes
- *               a subtree task when it is shallow enough (remaining depth
- *               <= task_depth, or <= 2 once a level holds min_tasks nodes),
- *               otherwise its children go to the next level
- *   k_perft_ws  persistent kernel, one worker per thread: tasks are dealt
- *               out as contiguous per-block ranges; a worker takes from its
- *               block's range and, when that is empty, steals from the
- *               other blocks' ranges (each range has one atomic cursor, so
- *               every task is taken exactly once and no wait is needed).
- *               A task is a depth-first walk whose last ply is counted with
- *               popcounts (count_legal), never expanded.
+ *               a subtree task when its remaining depth is <= task_depth
+ *               (lower only while a level holds fewer than min_tasks
+ *               nodes), otherwise its children go to the next level
+ *   k_perft_ws  persistent kernel, one worker per thread block: tasks are
+ *               dealt out as contiguous per-block ranges; a block takes
+ *               from its own range and, when that is empty, steals from
+ *               the other blocks' ranges (one atomic cursor per range, so
+ *               every task is taken exactly once and nothing waits).
+ *
+ * A block runs its task breadth-first: the task root's children go to
+ * shared memory, their children (the nodes one ply above the leaves) to a
+ * per-block scratch area that stays in L2, and then every thread of the
+ * block counts those nodes' legal moves with popcounts (count_legal)
+ * instead of expanding them.  The counting phase, which is nearly all of
+ * the work, runs with no divergence between threads.
  *
  * The sequence is captured in a CUDA graph and replayed while the batch
  * shape stays the same.  Leaf counts are u64 and summed with atomics, so
@@ -34,6 +39,7 @@ namespace {
 
 constexpr uint32_t ST_CAPACITY = 1u;
 constexpr uint32_t ST_DEPTH = 2u;
+constexpr int kMaxChildren = 218; /* most legal moves of any chess position */
 
 __device__ __forceinline__ Pos load_pos(const uint64_t *b) {
   Pos p;
@@ -71,14 +77,13 @@ __global__ void __launch_bounds__(128) k_split(int level, const Task *__restrict
                                                Task *__restrict__ fin, uint32_t cap_lvl, uint32_t cap_fin,
                                                uint32_t min_tasks, int rmax, PerftCounters *pc) {
   const uint32_t n_in = pc->level_n[level];
-  const int rmin = rmax < 2 ? rmax : 2;
   const bool last = level == kMaxLevels - 1;
   Move list[256];
   unsigned long long interior = 0;
   for (uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n_in; idx += gridDim.x * blockDim.x) {
     Task t = in[idx];
     int d = t.depth;
-    bool split = (d > rmax) || (n_in < min_tasks && d > rmin);
+    bool split = (d > rmax) || (n_in < min_tasks && d > 1);
     if (split && last) {
       atomicOr(&pc->status, ST_DEPTH);
       continue;
@@ -132,91 +137,153 @@ __device__ __forceinline__ bool take_task(uint32_t *cursors, uint32_t n, uint32_
   return false;
 }
 
+/* exclusive prefix sum over the block; returns the block total */
 template <int TPB>
-__global__ void __launch_bounds__(TPB) k_perft_ws(const Task *__restrict__ tasks, uint32_t *cursors,
-                                                  uint64_t *__restrict__ leaves, PerftCounters *pc) {
-  const uint32_t n = min(pc->n_final, 0xFFFFFFFFu);
+__device__ __forceinline__ int block_exclusive_scan(int v, int &excl, int *warp_tot) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) warp_tot[warp] = x;
+  __syncthreads();
+  int before = 0, total = 0;
+#pragma unroll
+  for (int w = 0; w < TPB / 32; w++) {
+    int t = warp_tot[w];
+    before += (w < warp) ? t : 0;
+    total += t;
+  }
+  excl = before + x - v;
+  __syncthreads();
+  return total;
+}
+
+template <int TPB>
+__device__ __forceinline__ unsigned long long block_sum(unsigned long long v, unsigned long long *red) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xFFFFFFFFu, v, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  unsigned long long s = 0;
+  if (threadIdx.x == 0)
+#pragma unroll
+    for (int w = 0; w < TPB / 32; w++) s += red[w];
+  __syncthreads();
+  return s;
+}
+
+/* One copy of each generator in the kernel's code: the kernels call them
+ * from several places, and inlining every call overflows the
+ * instruction cache. */
+__device__ __noinline__ int count_node(Pos p, int stm) { return count_legal(p, stm); }
+__device__ __noinline__ int expand_node(Pos p, int stm, Move *list) { return gen_legal(p, stm, false, list); }
+
+/* Expand src[0..nsrc) (nsrc <= TPB, one node per thread) into dst,
+ * children of a node contiguous; returns the number written.  Block-wide:
+ * every thread must call it. */
+template <int TPB>
+__device__ __forceinline__ int expand_round(const Pos *src, int nsrc, int stm, Pos *dst, int *s_warp, Move *list,
+                                            unsigned long long &interior) {
+  const int tid = threadIdx.x;
+  int k = 0;
+  if (tid < nsrc) {
+    k = expand_node(src[tid], stm, list);
+    interior++;
+  }
+  int off;
+  const int total = block_exclusive_scan<TPB>(k, off, s_warp);
+  for (int j = 0; j < k; j++) {
+    Pos c = src[tid];
+    play(c, list[j], true);
+    dst[off + j] = c;
+  }
+  __syncthreads();
+  return total;
+}
+
+/* sum of the legal-move counts of src[0..n): the leaf count below them */
+template <int TPB>
+__device__ __forceinline__ unsigned long long count_range(const Pos *src, int n, int stm, unsigned long long &counted) {
+  unsigned long long acc = 0;
+  for (int j = threadIdx.x; j < n; j += TPB) {
+    acc += (unsigned)count_node(src[j], stm);
+    counted++;
+  }
+  return acc;
+}
+
+/* Per-block scratch: `cap2` positions for a depth-4 task's second level
+ * (218*218 covers any position) and `cap3` for the nodes one ply above the
+ * leaves; each round expands at most cap3/218 parents, so it never
+ * overflows. */
+template <int TPB, int MINB>
+__global__ void __launch_bounds__(TPB, MINB) k_perft_ws(const Task *__restrict__ tasks, uint32_t *cursors,
+                                                  uint64_t *__restrict__ leaves, PerftCounters *pc,
+                                                  Pos *__restrict__ scratch, uint32_t cap2, uint32_t cap3) {
+  __shared__ Pos s_l1[256];
+  __shared__ Pos s_root;
+  __shared__ int s_warp[TPB / 32];
+  __shared__ unsigned long long s_red[TPB / 32];
+  __shared__ uint32_t s_task;
+
+  const int tid = threadIdx.x;
+  const uint32_t n = pc->n_final;
   const uint32_t B = gridDim.x;
+  const int per_round = min(TPB, (int)(cap3 / kMaxChildren));
+  Pos *b2 = scratch + (size_t)blockIdx.x * (cap2 + cap3);
+  Pos *b3 = b2 + cap2;
   uint32_t victim = 0;
   unsigned long long steals = 0, interior = 0, counted = 0;
-
-  Move l0[256], l1[256];
-  int n0 = 0, i0 = 0, n1 = 0, i1 = 0;
-  int R = -1;         /* remaining depth of the current task; -1 none, -2 count then finish */
-  Pos base, mid;
-  int sb = 0;
-  uint32_t root = 0;
-  unsigned long long acc = 0;
+  Move list[256];
 
   for (;;) {
-    Pos leaf;
-    int sl = 0;
-    bool have = false;
-    /* advance to the next node whose children are the leaves */
-    for (;;) {
-      if (R == -1) {
-        uint32_t idx;
-        if (!take_task(cursors, n, B, victim, idx, steals)) break;
-        Task t = tasks[idx];
-        base = t.pos;
-        sb = t.stm;
-        root = t.root;
-        R = t.depth;
-        acc = 0;
-        if (R == 0) {
-          atomicAdd((unsigned long long *)&leaves[root], 1ULL);
-          R = -1;
-          continue;
-        }
-        if (R == 1) {
-          leaf = base;
-          sl = sb;
-          R = -2;
-          have = true;
-          break;
-        }
-        n0 = gen_legal(base, sb, false, l0);
-        interior++;
-        i0 = 0;
-        n1 = 0;
-        i1 = 0;
-      }
+    if (tid == 0) {
+      uint32_t idx;
+      s_task = take_task(cursors, n, B, victim, idx, steals) ? idx : 0xFFFFFFFFu;
+    }
+    __syncthreads();
+    const uint32_t ti = s_task;
+    if (ti == 0xFFFFFFFFu) break;
+    const Task t = tasks[ti];
+    const int R = t.depth;
+    unsigned long long acc = 0;
+    if (tid == 0) s_root = t.pos;
+    __syncthreads();
+    if (R == 0) {
+      acc = tid == 0;
+    } else if (R == 1) {
+      acc = count_range<TPB>(&s_root, 1, t.stm, counted);
+    } else {
+      /* level 1: the task root's children, in shared memory */
+      const int n1 = expand_round<TPB>(&s_root, 1, t.stm, s_l1, s_warp, list, interior);
       if (R == 2) {
-        if (i0 < n0) {
-          leaf = base;
-          play(leaf, l0[i0++], true);
-          sl = sb ^ 1;
-          have = true;
-          break;
+        acc = count_range<TPB>(s_l1, n1, t.stm ^ 1, counted);
+      } else {
+        /* R == 4: level 2 in full into the block's level-2 buffer */
+        const Pos *par = s_l1;
+        int npar = n1, spar = t.stm ^ 1;
+        if (R == 4) {
+          int n2 = 0;
+          for (int base = 0; base < n1; base += TPB)
+            n2 += expand_round<TPB>(s_l1 + base, min(TPB, n1 - base), t.stm ^ 1, b2 + n2, s_warp, list, interior);
+          par = b2;
+          npar = n2;
+          spar = t.stm;
         }
-      } else if (R == 3) {
-        if (i1 < n1) {
-          leaf = mid;
-          play(leaf, l1[i1++], true);
-          sl = sb;
-          have = true;
-          break;
-        }
-        if (i0 < n0) {
-          mid = base;
-          play(mid, l0[i0++], true);
-          n1 = gen_legal(mid, sb ^ 1, false, l1);
-          interior++;
-          i1 = 0;
-          continue;
+        /* the nodes one ply above the leaves, a round at a time, then count */
+        for (int base = 0; base < npar; base += per_round) {
+          const int total = expand_round<TPB>(par + base, min(per_round, npar - base), spar, b3, s_warp, list,
+                                              interior);
+          acc += count_range<TPB>(b3, total, spar ^ 1, counted);
+          __syncthreads();
         }
       }
-      /* task done */
-      if (acc) atomicAdd((unsigned long long *)&leaves[root], acc);
-      R = -1;
     }
-    if (!have) break;
-    acc += (unsigned)count_legal(leaf, sl);
-    counted++;
-    if (R == -2) {
-      if (acc) atomicAdd((unsigned long long *)&leaves[root], acc);
-      R = -1;
-    }
+    const unsigned long long sum = block_sum<TPB>(acc, s_red);
+    if (tid == 0 && sum) atomicAdd((unsigned long long *)&leaves[t.root], sum);
   }
   /* warp-aggregate the statistics */
   for (int o = 16; o > 0; o >>= 1) {
@@ -224,8 +291,8 @@ __global__ void __launch_bounds__(TPB) k_perft_ws(const Task *__restrict__ tasks
     interior += __shfl_down_sync(0xFFFFFFFFu, interior, o);
     counted += __shfl_down_sync(0xFFFFFFFFu, counted, o);
   }
-  if ((threadIdx.x & 31) == 0) {
-    atomicAdd(&pc->steals, steals);
+  if ((tid & 31) == 0) {
+    if (steals) atomicAdd(&pc->steals, steals);
     atomicAdd(&pc->interior, interior);
     atomicAdd(&pc->counted, counted);
   }
@@ -242,14 +309,25 @@ __global__ void k_genmoves(const uint64_t *__restrict__ boards, const uint8_t *_
   for (int j = 0; j < k; j++) moves[(size_t)i * 256 + j] = list[j];
 }
 
-typedef void (*WsKernel)(const Task *, uint32_t *, uint64_t *, PerftCounters *);
+typedef void (*WsKernel)(const Task *, uint32_t *, uint64_t *, PerftCounters *, Pos *, uint32_t, uint32_t);
 
-WsKernel ws_kernel(int tpb) {
-  switch (tpb) {
-    case 64: return k_perft_ws<64>;
-    case 128: return k_perft_ws<128>;
-    case 256: return k_perft_ws<256>;
-    case 512: return k_perft_ws<512>;
+/* Compiled variants: threads per block x minimum resident blocks per SM
+ * (the second number caps registers per thread at 65536/(TPB*MINB));
+ * blocks_per_sm == 0 selects the uncapped variant. */
+WsKernel ws_kernel(int tpb, int minb) {
+  switch (tpb * 100 + minb) {
+    case 6400: return k_perft_ws<64, 1>;
+    case 6408: return k_perft_ws<64, 8>;
+    case 6412: return k_perft_ws<64, 12>;
+    case 12800: return k_perft_ws<128, 1>;
+    case 12804: return k_perft_ws<128, 4>;
+    case 12806: return k_perft_ws<128, 6>;
+    case 12808: return k_perft_ws<128, 8>;
+    case 25600: return k_perft_ws<256, 1>;
+    case 25603: return k_perft_ws<256, 3>;
+    case 25604: return k_perft_ws<256, 4>;
+    case 51200: return k_perft_ws<512, 1>;
+    case 51202: return k_perft_ws<512, 2>;
     default: return nullptr;
   }
 }
@@ -279,22 +357,32 @@ int perft_ensure_arena(uint64_t tasks_cap) {
 int perft_run(const uint64_t *d_boards, const uint8_t *d_stm, const uint8_t *d_depth, int n, uint64_t *d_leaves,
               cudaStream_t s);
 
-static int ws_geometry(int &blocks, int &tpb) {
+/* grid of the work-stealing kernel, cursors and per-block scratch */
+static int ws_geometry(int &blocks, int &tpb, WsKernel &k) {
   Context &c = ctx();
   tpb = c.pcfg.threads_per_block;
-  WsKernel k = ws_kernel(tpb);
-  if (!k) return set_error(ZETA_ERR_ARG, "threads_per_block must be 64, 128, 256 or 512");
-  int bps = c.pcfg.blocks_per_sm;
-  if (bps <= 0) {
-    ZCHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k, tpb, 0));
-    if (bps < 1) bps = 1;
-  }
+  k = ws_kernel(tpb, c.pcfg.blocks_per_sm);
+  if (!k)
+    return set_error(ZETA_ERR_ARG, "no perft kernel variant for %d threads x %d blocks per SM", tpb,
+                     c.pcfg.blocks_per_sm);
+  int bps = 0;
+  ZCHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k, tpb, 0));
+  if (bps < 1) bps = 1;
   blocks = c.sms * bps;
-  if (blocks > c.cursors_cap) {
+  const uint32_t cap2 = c.pcfg.task_depth >= 4 ? (uint32_t)(kMaxChildren * kMaxChildren) : 0u;
+  const uint32_t cap = cap2 + (uint32_t)tpb * kMaxChildren;
+  bool regrow = blocks > c.cursors_cap || (uint64_t)blocks * cap > c.scratch_cap;
+  if (regrow) {
     if (c.cursors) cudaFree(c.cursors);
+    if (c.scratch) cudaFree(c.scratch);
     c.cursors = nullptr;
+    c.scratch = nullptr;
+    c.cursors_cap = 0;
+    c.scratch_cap = 0;
     ZCHECK(cudaMalloc(&c.cursors, blocks * sizeof(uint32_t)));
     c.cursors_cap = blocks;
+    ZCHECK(cudaMalloc(&c.scratch, (size_t)blocks * cap * sizeof(Pos)));
+    c.scratch_cap = (uint64_t)blocks * cap;
     if (c.graph) {
       cudaGraphExecDestroy(c.graph);
       c.graph = nullptr;
@@ -305,9 +393,9 @@ static int ws_geometry(int &blocks, int &tpb) {
 
 /* enqueue the whole launch sequence on `s` */
 static int perft_enqueue(const uint64_t *d_boards, const uint8_t *d_stm, const uint8_t *d_depth, int n,
-                         uint64_t *d_leaves, cudaStream_t s, int blocks, int tpb, bool timed, bool capturing) {
+                         uint64_t *d_leaves, cudaStream_t s, int blocks, int tpb, WsKernel k, bool capturing) {
   Context &c = ctx();
-  uint32_t min_tasks = c.pcfg.min_tasks ? c.pcfg.min_tasks : (uint32_t)(4ull * blocks * tpb);
+  const uint32_t min_tasks = c.pcfg.min_tasks; /* 0: never split below task_depth */
   ZCHECK(cudaMemsetAsync(c.pc, 0, sizeof(PerftCounters), s));
   ZCHECK(cudaMemsetAsync(c.cursors, 0, blocks * sizeof(uint32_t), s));
   k_roots<<<(n + 127) / 128, 128, 0, s>>>(d_boards, d_stm, d_depth, n, c.lvl[0], d_leaves, c.pc);
@@ -318,11 +406,12 @@ static int perft_enqueue(const uint64_t *d_boards, const uint8_t *d_stm, const u
     ZCHECK(cudaGetLastError());
   }
   /* external records: inside a stream capture they become event-record
-   * nodes of the graph, so the kernel can be timed on every replay */
-  if (timed) ZCHECK(capturing ? cudaEventRecordWithFlags(c.ev[1], s, cudaEventRecordExternal) : cudaEventRecord(c.ev[1], s));
-  ws_kernel(tpb)<<<blocks, tpb, 0, s>>>(c.fin, c.cursors, d_leaves, c.pc);
+   * nodes of the graph, so the kernel is timed on every replay */
+  ZCHECK(capturing ? cudaEventRecordWithFlags(c.ev[1], s, cudaEventRecordExternal) : cudaEventRecord(c.ev[1], s));
+  const uint32_t cap2 = c.pcfg.task_depth >= 4 ? (uint32_t)(kMaxChildren * kMaxChildren) : 0u;
+  k<<<blocks, tpb, 0, s>>>(c.fin, c.cursors, d_leaves, c.pc, c.scratch, cap2, (uint32_t)tpb * kMaxChildren);
   ZCHECK(cudaGetLastError());
-  if (timed) ZCHECK(capturing ? cudaEventRecordWithFlags(c.ev[2], s, cudaEventRecordExternal) : cudaEventRecord(c.ev[2], s));
+  ZCHECK(capturing ? cudaEventRecordWithFlags(c.ev[2], s, cudaEventRecordExternal) : cudaEventRecord(c.ev[2], s));
   return ZETA_OK;
 }
 
@@ -351,9 +440,10 @@ int perft_launch(const uint64_t *d_boards, const uint8_t *d_stm, const uint8_t *
 int perft_run(const uint64_t *d_boards, const uint8_t *d_stm, const uint8_t *d_depth, int n, uint64_t *d_leaves,
               cudaStream_t s) {
   Context &c = ctx();
-  if (c.pcfg.task_depth < 1 || c.pcfg.task_depth > 3) return set_error(ZETA_ERR_ARG, "task_depth must be 1..3");
+  if (c.pcfg.task_depth < 1 || c.pcfg.task_depth > 4) return set_error(ZETA_ERR_ARG, "task_depth must be 1..4");
   int blocks, tpb;
-  int rc = ws_geometry(blocks, tpb);
+  WsKernel k;
+  int rc = ws_geometry(blocks, tpb, k);
   if (rc) return rc;
   if (c.cap_fin == 0) {
     rc = perft_ensure_arena(8u << 20);
@@ -373,7 +463,7 @@ int perft_run(const uint64_t *d_boards, const uint8_t *d_stm, const uint8_t *d_d
       }
       cudaGraph_t g;
       ZCHECK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-      rc = perft_enqueue(d_boards, d_stm, d_depth, n, d_leaves, s, blocks, tpb, true, true);
+      rc = perft_enqueue(d_boards, d_stm, d_depth, n, d_leaves, s, blocks, tpb, k, true);
       cudaError_t e = cudaStreamEndCapture(s, &g);
       if (rc) return rc;
       if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
@@ -390,7 +480,7 @@ int perft_run(const uint64_t *d_boards, const uint8_t *d_stm, const uint8_t *d_d
     }
     ZCHECK(cudaGraphLaunch(c.graph, s));
   } else {
-    rc = perft_enqueue(d_boards, d_stm, d_depth, n, d_leaves, s, blocks, tpb, true, false);
+    rc = perft_enqueue(d_boards, d_stm, d_depth, n, d_leaves, s, blocks, tpb, k, false);
     if (rc) return rc;
   }
   ZCHECK(cudaEventRecord(c.ev[3], s));
@@ -406,7 +496,7 @@ int perft_run(const uint64_t *d_boards, const uint8_t *d_stm, const uint8_t *d_d
   (void)cudaGetLastError(); /* a failed timing query must not poison the next call */
   if (h.status & ST_CAPACITY) {
     /* grow the arena for the next call and report */
-    uint64_t need = std::max<uint64_t>(h.n_final, 0);
+    uint64_t need = h.n_final;
     for (int i = 0; i <= kMaxLevels; i++) need = std::max<uint64_t>(need, h.level_n[i]);
     perft_ensure_arena(need + need / 4 + 1024);
     return set_error(ZETA_ERR_CAPACITY, "perft task arena too small (%llu tasks needed); grown, retry",
@@ -433,21 +523,23 @@ int genmoves_launch(const uint64_t *d_boards, const uint8_t *d_stm, int n, int q
  * may synchronise the whole device -- is not acceptable.  For them,
  * zeta_perft_batch_noalloc runs the same launch sequence as
  * zeta_perft_batch_device with all of its scratch (task arrays, counters,
- * work-stealing cursors) in one fixed file-scope device array instead of
- * buffers allocated by the library.  The caller passes the inputs and
- * outputs, already in device memory. */
+ * work-stealing cursors, per-block node buffers) in one fixed file-scope
+ * device array instead of buffers allocated by the library.  The caller
+ * passes the inputs and outputs, already in device memory. */
 namespace {
 constexpr uint32_t kNoAllocMaxTasks = 1u << 17; /* per task array: 131072 subtrees */
-constexpr int kNoAllocMaxBlocks = 4096;         /* work-stealing cursors */
+constexpr int kNoAllocMaxBlocks = 256;          /* worker blocks */
+constexpr uint32_t kNoAllocNodesPerBlock = 1024; /* per-block node buffer */
 
 struct NoAllocScratch {
   PerftCounters pc;
   uint32_t cursors[kNoAllocMaxBlocks];
   Task lvl[2][kNoAllocMaxTasks];
   Task fin[kNoAllocMaxTasks];
+  Pos nodes[kNoAllocMaxBlocks * kNoAllocNodesPerBlock];
 };
 
-/* about 19 MB; every GPU that loads the library holds it until exit */
+/* about 29 MB; every GPU that loads the library holds it until exit */
 static __device__ __align__(256) unsigned char g_noalloc_scratch[sizeof(NoAllocScratch)];
 
 constexpr int kNoAllocMaxDevices = 64;
@@ -475,7 +567,7 @@ extern "C" int zeta_perft_batch_noalloc(const uint64_t *d_boards, const uint8_t 
     ZCHECK(cudaGetSymbolAddress(&p, g_noalloc_scratch));
     int sms = 0, bps = 0;
     ZCHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    ZCHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_perft_ws<128>, 128, 0));
+    ZCHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_perft_ws<128, 1>, 128, 0));
     int blocks = sms * (bps > 0 ? bps : 1);
     if (blocks > kNoAllocMaxBlocks) blocks = kNoAllocMaxBlocks;
     g_noalloc_sms[dev] = sms;
@@ -488,18 +580,15 @@ extern "C" int zeta_perft_batch_noalloc(const uint64_t *d_boards, const uint8_t 
   /* the array keeps the previous call's contents: clear what must start at zero */
   ZCHECK(cudaMemsetAsync(&S->pc, 0, sizeof(PerftCounters), s));
   ZCHECK(cudaMemsetAsync(S->cursors, 0, blocks * sizeof(uint32_t), s));
-  /* stop splitting early enough that the next level (about 35 children per
-   * node) still fits the fixed task arrays */
-  uint32_t min_tasks = (uint32_t)(4ull * blocks * 128);
-  if (min_tasks > kNoAllocMaxTasks / 64) min_tasks = kNoAllocMaxTasks / 64;
   k_roots<<<(n + 127) / 128, 128, 0, s>>>(d_boards, d_stm, d_depth, n, S->lvl[0], d_leaves, &S->pc);
   ZCHECK(cudaGetLastError());
   for (int lv = 0; lv < kMaxLevels; lv++) {
     k_split<<<sms * 4, 128, 0, s>>>(lv, S->lvl[lv & 1], S->lvl[(lv + 1) & 1], S->fin, kNoAllocMaxTasks,
-                                    kNoAllocMaxTasks, min_tasks, 3, &S->pc);
+                                    kNoAllocMaxTasks, 0u, 3, &S->pc);
     ZCHECK(cudaGetLastError());
   }
-  k_perft_ws<128><<<blocks, 128, 0, s>>>(S->fin, S->cursors, d_leaves, &S->pc);
+  k_perft_ws<128, 1><<<blocks, 128, 0, s>>>(S->fin, S->cursors, d_leaves, &S->pc, S->nodes, 0u,
+                                            kNoAllocNodesPerBlock);
   ZCHECK(cudaGetLastError());
   uint32_t status = 0;
   ZCHECK(cudaMemcpyAsync(&status, &S->pc.status, sizeof status, cudaMemcpyDeviceToHost, s));
