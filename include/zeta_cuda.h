@@ -115,6 +115,26 @@ typedef struct {
 int zeta_perft_last_stats(zeta_perft_stats *st);
 
 /* ------------------------------------------------------------------ */
+/* Batched fixed-depth search ("pure" alpha-beta): legal moves, the
+ * reference evaluation (zeta.cl:1479-1554) at the leaves, mate -INF+ply,
+ * stalemate 0, no quiescence/extensions/pruning/draw rules, so each root
+ * score equals plain negamax.  `workers` ABDADA workers per position share
+ * the transposition table (zeta_init's tt1, kept between calls; entries
+ * are used only at equal remaining depth, so stale entries stay correct).
+ * Replaces the fixed-depth use of cl_run_alphabeta (src/clrun.c:675-974)
+ * for a batch.  Outputs: score from the side to move, a best move (one
+ * that reaches the score), visited nodes summed over the workers. */
+int zeta_search_batch(const uint64_t *boards, const uint8_t *stm, int n, int depth, int workers, int32_t *scores,
+                      uint32_t *bestmoves, uint64_t *nodes);
+/* same with device buffers, on `stream` (NULL = the library's stream) */
+int zeta_search_batch_device(const uint64_t *d_boards, const uint8_t *d_stm, int n, int depth, int workers,
+                             int32_t *d_scores, uint32_t *d_bestmoves, uint64_t *d_nodes, void *stream);
+/* zero the transposition tables (as a new game does, src/xboard.c:159-199) */
+int zeta_tt_clear(void);
+/* device time of the last search kernel, ms */
+int zeta_search_last_ms(float *kernel_ms);
+
+/* ------------------------------------------------------------------ */
 /* Seeded synthetic positions generated on the device (the benchmark
  * workloads): position i is a pure function of (seed, i), see
  * zeta_gb300/csrc/positions.cu.  Host buffers: boards n*7, stm n,

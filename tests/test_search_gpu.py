@@ -1,0 +1,84 @@
+"""Batched pure fixed-depth search on the GB300 against the oracle's plain
+negamax / alpha-beta (integer scores: exact equality)."""
+import numpy as np
+import pytest
+
+import oracle_lib as ol
+
+pytestmark = pytest.mark.gpu
+
+
+def _positions(seed, n, lo=10, hi=60, pieces=0):
+    return ol.make_positions(seed, n, min_plies=lo, max_plies=hi, min_pieces=pieces, min_depth=0, max_depth=0)
+
+
+@pytest.mark.parametrize("depth", [1, 2, 3, 4])
+def test_root_scores_equal_negamax(zeta_device, depth):
+    z = zeta_device
+    boards, stm, _ = _positions(0x5EA7C0 + depth, 96, 1, 120)
+    for workers in (1, 4):
+        z.tt_clear()
+        scores, moves, nodes = z.search_batch(boards, stm, depth, workers)
+        for i in range(len(stm)):
+            v, _, _ = ol.alphabeta(boards[i], stm[i], depth)
+            assert scores[i] == v, (i, depth, workers, scores[i], v)
+        assert (nodes > 0).all()
+
+
+def test_best_move_reaches_the_score(zeta_device):
+    z = zeta_device
+    depth = 3
+    boards, stm, _ = _positions(0xB357, 48, 10, 60)
+    z.tt_clear()
+    scores, moves, _ = z.search_batch(boards, stm, depth, 4)
+    for i in range(len(stm)):
+        legal = ol.genmoves(boards[i], stm[i])
+        assert moves[i] in legal
+        child = ol.play(boards[i], stm[i], int(moves[i]))
+        v, _, _ = ol.alphabeta(child, 1 - stm[i], depth - 1)
+        # the child is one ply deeper: shift its mate distance by one ply
+        if abs(v) > 30000:
+            v = v - 1 if v > 0 else v + 1
+        assert -v == scores[i], i
+
+
+def test_mate_and_stalemate_scores(zeta_device):
+    z = zeta_device
+    mate_in_1, s1 = ol.setboard("6k1/5ppp/8/8/8/8/5PPP/3R2K1 w - - 0 1")   # Rd8#
+    mated, s2 = ol.setboard("rnb1kbnr/pppp1ppp/8/4p3/6Pq/5P2/PPPPP2P/RNBQKBNR w KQkq - 1 3")
+    stale, s3 = ol.setboard("7k/5Q2/6K1/8/8/8/8/8 b - - 0 1")
+    boards = np.stack([mate_in_1, mated, stale])
+    stm = np.array([s1, s2, s3], np.uint8)
+    for depth in (1, 2, 3):
+        z.tt_clear()
+        scores, _, _ = z.search_batch(boards, stm, depth, 2)
+        want = [ol.alphabeta(boards[i], stm[i], depth)[0] for i in range(3)]
+        assert list(scores) == want, depth
+    assert want[0] == 32000 - 1 and want[1] == -32000 and want[2] == 0
+
+
+def test_deeper_search_matches_oracle_and_worker_counts_agree(zeta_device):
+    z = zeta_device
+    boards, stm, _ = _positions(0xD5, 6, 20, 40, 20)
+    want = [ol.alphabeta(boards[i], stm[i], 5)[0] for i in range(len(stm))]
+    for workers in (1, 3, 8, 16):
+        z.tt_clear()
+        scores, _, _ = z.search_batch(boards, stm, 5, workers)
+        assert list(scores) == want, workers
+    # a warm table (entries of the previous calls) does not change values
+    scores, _, _ = z.search_batch(boards, stm, 5, 8)
+    assert list(scores) == want
+
+
+def test_benchmark_workload_depth7_is_worker_independent(zeta_device):
+    """Full benchmark depth on a sample: values agree across worker counts
+    and with a cold or warm table (size-independent check)."""
+    z = zeta_device
+    w = z.WORKLOADS["search_batch"]
+    boards, stm, _ = z.make_positions(w["seed"], 64, w["min_plies"], w["max_plies"], w["min_pieces"], 0, 0)
+    z.tt_clear()
+    a, _, _ = z.search_batch(boards, stm, 7, 1)
+    z.tt_clear()
+    b, _, _ = z.search_batch(boards, stm, 7, 8)
+    c, _, _ = z.search_batch(boards, stm, 7, 8)
+    assert np.array_equal(a, b) and np.array_equal(b, c)

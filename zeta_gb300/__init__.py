@@ -83,6 +83,12 @@ SIGNATURES = {
     "zeta_make_positions": (ctypes.c_int, [ctypes.c_uint64, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                            ctypes.c_int, ctypes.c_int, _u64p, _u8p, _u8p]),
     "zeta_int_peak": (ctypes.c_int, [ctypes.POINTER(ctypes.c_double)]),
+    "zeta_search_batch": (ctypes.c_int, [_u64p, _u8p, ctypes.c_int, ctypes.c_int, ctypes.c_int, _i32p, _u32p, _u64p]),
+    "zeta_search_batch_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                                                ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                                ctypes.c_void_p]),
+    "zeta_tt_clear": (ctypes.c_int, []),
+    "zeta_search_last_ms": (ctypes.c_int, [ctypes.POINTER(ctypes.c_float)]),
     "zeta_genmoves_batch": (ctypes.c_int, [_u64p, _u8p, ctypes.c_int, ctypes.c_int, _u32p, _i32p]),
 }
 
@@ -183,6 +189,35 @@ def make_positions(seed: int, n: int, min_plies: int, max_plies: int, min_pieces
     _check(load_library().zeta_make_positions(seed & (2**64 - 1), n, min_plies, max_plies, min_pieces, min_depth,
                                               max_depth, _ptr(boards, _u64p), _ptr(stm, _u8p), _ptr(depth, _u8p)))
     return boards, stm, depth
+
+
+def search_batch(boards: np.ndarray, stm: np.ndarray, depth: int, workers: int = 1):
+    """Fixed-depth pure alpha-beta: (scores, best moves, nodes) per position."""
+    b = np.ascontiguousarray(boards, dtype=np.uint64).reshape(-1, 7)
+    s = np.ascontiguousarray(stm, dtype=np.uint8)
+    n = b.shape[0]
+    scores = np.zeros(n, dtype=np.int32)
+    moves = np.zeros(n, dtype=np.uint32)
+    nodes = np.zeros(n, dtype=np.uint64)
+    _check(load_library().zeta_search_batch(_ptr(b, _u64p), _ptr(s, _u8p), n, depth, workers, _ptr(scores, _i32p),
+                                            _ptr(moves, _u32p), _ptr(nodes, _u64p)))
+    return scores, moves, nodes
+
+
+def search_batch_device(d_boards: int, d_stm: int, n: int, depth: int, workers: int, d_scores: int, d_moves: int,
+                        d_nodes: int, stream: int = 0) -> None:
+    _check(load_library().zeta_search_batch_device(d_boards, d_stm, n, depth, workers, d_scores, d_moves, d_nodes,
+                                                   stream or None))
+
+
+def tt_clear() -> None:
+    _check(load_library().zeta_tt_clear())
+
+
+def search_last_ms() -> float:
+    t = ctypes.c_float()
+    _check(load_library().zeta_search_last_ms(ctypes.byref(t)))
+    return t.value
 
 
 def int_peak_tops() -> float:

@@ -29,7 +29,7 @@ REFERENCE_SRC = "/root/reference/src"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"] + ARCH
 
-CUDA_SOURCES = ["capi.cu", "perft.cu", "positions.cu", "peak.cu"]
+CUDA_SOURCES = ["capi.cu", "perft.cu", "positions.cu", "peak.cu", "search.cu"]
 OPTIONAL_CUDA_SOURCES = ["search.cu", "mlp.cu", "noalloc.cu"]
 HOST_SOURCES = ["board.c", "cudarun.c", "engine.c", "xboard.c", "main.c"]
 
@@ -64,7 +64,8 @@ def _headers() -> list[str]:
 def build_cuda(verbose: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
     nvcc = _nvcc()
-    sources = CUDA_SOURCES + [s for s in OPTIONAL_CUDA_SOURCES if os.path.exists(os.path.join(CSRC, s))]
+    sources = CUDA_SOURCES + [s for s in OPTIONAL_CUDA_SOURCES
+                              if s not in CUDA_SOURCES and os.path.exists(os.path.join(CSRC, s))]
     headers = _headers()
     objs = []
     jobs = []

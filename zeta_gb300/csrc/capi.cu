@@ -129,6 +129,11 @@ int zeta_release(void) {
   if (c.h_pinned) cudaFreeHost(c.h_pinned);
   cudaFree(c.tt1);
   cudaFree(c.tt2);
+  cudaFree(c.s_out);
+  cudaFree(c.s_done);
+  cudaFree(c.s_busy);
+  cudaFree(c.s_status);
+  cudaFree(c.s_tt);
   for (int i = 0; i < 4; i++)
     if (c.ev[i]) cudaEventDestroy(c.ev[i]);
   for (int i = 0; i < 2; i++)
@@ -251,6 +256,61 @@ int zeta_int_peak(double *tops) {
   if (rc) return rc;
   if (!tops) return set_error(ZETA_ERR_ARG, "null pointer");
   return int_peak(tops);
+}
+
+int zeta_search_batch_device(const uint64_t *d_boards, const uint8_t *d_stm, int n, int depth, int workers,
+                             int32_t *d_scores, uint32_t *d_bestmoves, uint64_t *d_nodes, void *stream) {
+  int rc = require_ready();
+  if (rc) return rc;
+  if (!d_boards || !d_stm) return set_error(ZETA_ERR_ARG, "null buffer");
+  cudaStream_t s = stream ? (cudaStream_t)stream : g_ctx.stream;
+  return search_pure_launch(d_boards, d_stm, n, depth, workers, d_scores, d_bestmoves, (unsigned long long *)d_nodes,
+                            s);
+}
+
+int zeta_search_batch(const uint64_t *boards, const uint8_t *stm, int n, int depth, int workers, int32_t *scores,
+                      uint32_t *bestmoves, uint64_t *nodes) {
+  int rc = require_ready();
+  if (rc) return rc;
+  if (!boards || !stm || n <= 0) return set_error(ZETA_ERR_ARG, "bad batch arguments");
+  Context &c = g_ctx;
+  uint64_t *db = nullptr, *dn = nullptr;
+  uint8_t *ds = nullptr;
+  int32_t *dsc = nullptr;
+  uint32_t *dm = nullptr;
+  cudaError_t e = cudaMalloc(&db, (size_t)n * 56);
+  if (e == cudaSuccess) e = cudaMalloc(&ds, n);
+  if (e == cudaSuccess) e = cudaMalloc(&dsc, (size_t)n * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&dm, (size_t)n * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&dn, (size_t)n * 8);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(db, boards, (size_t)n * 56, cudaMemcpyHostToDevice, c.stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(ds, stm, n, cudaMemcpyHostToDevice, c.stream);
+  if (e == cudaSuccess) rc = search_pure_launch(db, ds, n, depth, workers, dsc, dm, (unsigned long long *)dn, c.stream);
+  if (e == cudaSuccess && rc == ZETA_OK && scores) e = cudaMemcpy(scores, dsc, (size_t)n * 4, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && rc == ZETA_OK && bestmoves) e = cudaMemcpy(bestmoves, dm, (size_t)n * 4, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && rc == ZETA_OK && nodes) e = cudaMemcpy(nodes, dn, (size_t)n * 8, cudaMemcpyDeviceToHost);
+  cudaFree(db);
+  cudaFree(ds);
+  cudaFree(dsc);
+  cudaFree(dm);
+  cudaFree(dn);
+  if (e != cudaSuccess) return cuda_fail(e, "zeta_search_batch");
+  return rc;
+}
+
+int zeta_tt_clear(void) {
+  int rc = require_ready();
+  if (rc) return rc;
+  rc = search_tt_clear(g_ctx.stream);
+  if (rc) return rc;
+  ZCHECK(cudaStreamSynchronize(g_ctx.stream));
+  return ZETA_OK;
+}
+
+int zeta_search_last_ms(float *kernel_ms) {
+  if (!kernel_ms) return set_error(ZETA_ERR_ARG, "null pointer");
+  *kernel_ms = g_ctx.sstats.kernel_ms;
+  return ZETA_OK;
 }
 
 int zeta_genmoves_batch(const uint64_t *boards, const uint8_t *stm, int n, int qs, uint32_t *moves, int32_t *counts) {

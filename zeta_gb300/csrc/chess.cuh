@@ -315,9 +315,10 @@ ZHD u64 slider_targets(const Sets &s, const Guard &g, u64 tgt) {
 /* ---------------- bulk count ----------------
  * Number of legal moves: the leaf count of a node one ply above the
  * leaves, without expanding it. */
-ZHD int count_legal(const Pos &p, int stm) {
+ZHD int count_legal_ex(const Pos &p, int stm, bool &in_check) {
   Sets s = make_sets(p, stm);
   Guard g = make_guard(s, stm);
+  in_check = (bool)(g.checkers != 0);
   u64 danger = enemy_attacks(s, stm);
   u64 tgt = ~s.us & g.cmask;
   int n = popc(king_attacks(s.kbb) & ~s.us & ~danger);
@@ -356,6 +357,11 @@ ZHD int count_legal(const Pos &p, int stm) {
   int e = ep_legal(p, s, stm, sqep);
   n += (e & 1) + (e >> 1);
   return n;
+}
+
+ZHD int count_legal(const Pos &p, int stm) {
+  bool in_check;
+  return count_legal_ex(p, stm, in_check);
 }
 
 /* ---------------- make ----------------

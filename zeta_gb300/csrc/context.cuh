@@ -66,7 +66,8 @@ struct Context {
   void *h_pinned = nullptr;
   size_t h_pinned_bytes = 0;
 
-  zeta_perft_config pcfg{128, 0, 0, 3, 1};
+  /* the autotuner's choice on GB300 (zeta_gb300/perft_tuned.json) */
+  zeta_perft_config pcfg{256, 3, 0, 4, 1};
   zeta_perft_stats pstats{};
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   cudaEvent_t ev_join[2] = {nullptr, nullptr}; /* ordering with a caller's stream */
@@ -81,6 +82,19 @@ struct Context {
   /* transposition tables (search) */
   void *tt1 = nullptr, *tt2 = nullptr;
   uint64_t tt1_entries = 0, tt2_entries = 0;
+
+  /* batched search */
+  void *s_out = nullptr;      /* per-position results */
+  uint32_t *s_done = nullptr; /* early-bird flags */
+  int s_cap = 0;
+  uint32_t *s_busy = nullptr; /* ABDADA busy table */
+  uint64_t s_busy_entries = 0;
+  uint32_t *s_status = nullptr;
+  void *s_tt = nullptr;       /* used when zeta_init made no table */
+  uint64_t s_tt_entries = 0;
+  struct {
+    float kernel_ms = -1.f;
+  } sstats;
 };
 
 Context &ctx();
@@ -100,6 +114,10 @@ int perft_ensure_arena(uint64_t tasks_cap);
 int positions_launch(u64 seed, int n, int min_plies, int max_plies, int min_pieces, int min_depth, int max_depth,
                      uint64_t *d_boards, uint8_t *d_stm, uint8_t *d_depth, uint32_t *d_fail, cudaStream_t s);
 int int_peak(double *tops);
+/* search.cu */
+int search_pure_launch(const uint64_t *d_boards, const uint8_t *d_stm, int n, int depth, int workers, int32_t *d_scores,
+                       uint32_t *d_moves, unsigned long long *d_nodes, cudaStream_t s);
+int search_tt_clear(cudaStream_t s);
 int genmoves_launch(const uint64_t *d_boards, const uint8_t *d_stm, int n, int qs, uint32_t *d_moves,
                     int32_t *d_counts, cudaStream_t stream);
 

@@ -1,0 +1,438 @@
+/*
+ * search.cu -- batched fixed-depth alpha-beta on GB300 ("pure" mode).
+ *
+ * The reference has no pure search: its alphabeta_gpu (zeta.cl:852-2512)
+ * always runs quiescence, extensions, null move, LMR and IID.  This kernel
+ * is the plain fixed-depth negamax the project defines for exact parity:
+ * legal moves (queen-only promotions), the reference's evaluation at the
+ * leaves from the side to move, mate = -INF+ply, stalemate = 0, no
+ * quiescence, extensions, pruning or draw rules.  The root value equals
+ * plain negamax exactly; alpha-beta, the transposition table and ABDADA
+ * only change how much of the tree is visited.
+ *
+ * Layout and parallelism
+ *  - One thread is one search worker.  A batch of N positions runs with W
+ *    workers each: thread t works on position t % N as worker t / N, so
+ *    the 32 lanes of a warp search 32 different positions and the workers
+ *    of one position sit in different warps (ABDADA across warps).
+ *  - Workers of a position share a 16-byte-entry transposition table in
+ *    HBM (1 GiB by default, 2^26 entries, shared by the whole batch):
+ *    {key ^ data, data}, data = move | score<<32 | depth<<48 | bound<<56,
+ *    written and read as one 16-byte access; a torn entry fails the XOR
+ *    check (the reference's lockless scheme, zeta.cl:1631,1891).  An entry
+ *    is used only at exactly the same remaining depth, which keeps the
+ *    result equal to plain negamax.
+ *  - ABDADA (Weill 1996; the reference's variant is zeta.cl:1648-1782): a
+ *    node of remaining depth >= 2 counts the workers inside it in a busy
+ *    table; a worker asked to search a younger brother exclusively skips it
+ *    while another worker is inside and comes back to it in a second pass.
+ *  - The first worker to finish a root publishes score, best move and
+ *    node counts; the others of that position see the flag and stop
+ *    (the reference's early-bird `finito`, zeta.cl:1790-1792).
+ *  - Every per-thread loop has a node budget; running out sets
+ *    ZETA_ERR_BUDGET in the status word instead of spinning.
+ */
+#include <cstdio>
+
+#include "context.cuh"
+#include "eval.cuh"
+#include "tables.cuh"
+
+namespace zeta {
+
+namespace {
+
+constexpr int kSearchInf = 32000;       /* INF, zeta.cl:131 */
+constexpr int kMate = 30000;            /* MATESCORE */
+constexpr int kOnEval = 32500;          /* "searched by another worker" */
+constexpr int kMaxSearchDepth = 16;
+constexpr int kMaxMoves = 218;
+constexpr int kAbdadaMinDepth = 2;
+constexpr uint32_t kDone = 1u << 30;    /* move flags above the 30-bit packing */
+constexpr uint32_t kDefer = 1u << 31;
+constexpr uint32_t kMoveBits = (1u << 30) - 1;
+
+constexpr uint32_t SST_BUDGET = 1u;
+
+enum Bound : uint32_t { B_NONE = 0, B_LOWER = 1, B_UPPER = 2, B_EXACT = 3 };
+
+/* exact castle rights and the en-passant square mixed into the reference
+ * Zobrist hash: its castle keys depend on either of the king and rook
+ * flags, which two positions with different rights can share */
+__device__ __forceinline__ u64 search_key(const Pos &p, int stm) {
+  u64 k = compute_hash(p, stm);
+  u64 cr = ~p.cr;
+  uint32_t rights = ((cr & ZETA_CR_WQ) == ZETA_CR_WQ) | (((cr & ZETA_CR_WK) == ZETA_CR_WK) << 1) |
+                    (((cr & ZETA_CR_BQ) == ZETA_CR_BQ) << 2) | (((cr & ZETA_CR_BK) == ZETA_CR_BK) << 3);
+  return k ^ ((u64)rights * 0x9E3779B97F4A7C15ULL);
+}
+
+struct TTEntry {
+  unsigned long long kx, data;
+};
+
+__device__ __forceinline__ bool tt_probe(const TTEntry *tt, u64 mask, u64 key, int &score, int &depth, int &bound,
+                                         Move &move) {
+  const longlong2 e = __ldcg((const longlong2 *)&tt[key & mask]);
+  const u64 kx = (u64)e.x, data = (u64)e.y;
+  if ((kx ^ data) != key) return false;
+  move = (Move)(data & 0xFFFFFFFFu);
+  score = (int)(int16_t)((data >> 32) & 0xFFFF);
+  depth = (int)((data >> 48) & 0xFF);
+  bound = (int)(data >> 56);
+  return true;
+}
+
+__device__ __forceinline__ void tt_store(TTEntry *tt, u64 mask, u64 key, int score, int depth, int bound, Move move) {
+  u64 data = (u64)(move & kMoveBits) | ((u64)(uint16_t)(int16_t)score << 32) | ((u64)(depth & 0xFF) << 48) |
+             ((u64)bound << 56);
+  longlong2 e;
+  e.x = (long long)(key ^ data);
+  e.y = (long long)data;
+  __stcg((longlong2 *)&tt[key & mask], e);
+}
+
+/* mate scores are kept relative to the node in the table */
+__device__ __forceinline__ int to_tt(int s, int ply) { return s > kMate ? s + ply : (s < -kMate ? s - ply : s); }
+__device__ __forceinline__ int from_tt(int s, int ply) { return s > kMate ? s - ply : (s < -kMate ? s + ply : s); }
+
+/* Move ordering: TT move, captures by MVV-LVA, queen promotions, the two
+ * killers of the ply, then quiet moves by piece-square gain -- the
+ * reference's scheme (zeta.cl:2039-2110) without the counter-move and
+ * randomisation terms. */
+__device__ __forceinline__ int order_score(Move m, int stm, Move ttmove, Move k0, Move k1, const EvalTables &T) {
+  if (m == ttmove) return 1 << 20;
+  int pf = m_pfrom(m) >> 1, pt = m_pto(m) >> 1, pc = m_pcpt(m) >> 1;
+  if (pc) return (1 << 18) + T.value[pc] * 16 - T.value[pt];
+  if (pt != pf) return (1 << 17);
+  if (m == k0) return (1 << 16) + 1;
+  if (m == k1) return (1 << 16);
+  int to = m_to(m), from = m_from(m);
+  int vt = stm ? to : (to ^ 56), vf = stm ? from : (from ^ 56);
+  return T.pst[pt][vt] + T.control[vt] - T.pst[pf][vf] - T.control[vf];
+}
+
+/* one ply of a worker's explicit stack */
+struct Frame {
+  Pos pos;
+  u64 key;
+  int alpha, beta, alpha0, best;
+  Move bestmove;
+  int n, i, iter, searched;
+  int depth;
+  uint8_t stm, exclusive, deferred, busy;
+  Move moves[kMaxMoves];
+};
+
+struct SearchOut {
+  int score;
+  Move bestmove;
+  unsigned long long nodes;
+  unsigned long long tthits;
+};
+
+/* single out-of-line copies (instruction cache, as in perft.cu) */
+__device__ __noinline__ int s_count(Pos p, int stm, bool *chk) {
+  bool c;
+  int n = count_legal_ex(p, stm, c);
+  *chk = c;
+  return n;
+}
+__device__ __noinline__ int s_gen(Pos p, int stm, Move *list) { return gen_legal(p, stm, false, list); }
+__device__ __noinline__ int s_eval(Pos p, const EvalTables *T) { return eval_white(p, *T); }
+
+/* value of a node with no depth left, from the side to move */
+__device__ __forceinline__ int leaf_value(const Pos &p, int stm, int ply, const EvalTables *T) {
+  bool chk;
+  if (s_count(p, stm, &chk) == 0) return chk ? -kSearchInf + ply : 0;
+  int e = s_eval(p, T);
+  return stm ? -e : e;
+}
+
+struct Worker {
+  TTEntry *tt;
+  u64 tt_mask;
+  uint32_t *busy;
+  u64 busy_mask;
+  const EvalTables *T;
+  unsigned long long nodes, tthits;
+  Move killer[kMaxSearchDepth + 1][2];
+  int scores[kMaxMoves];
+};
+
+/* Set up frame f at `ply`; false when the node is decided on entry (TT
+ * hit, busy elsewhere, no legal move), with its value in `value` (kOnEval
+ * for an exclusive request on a busy node). */
+__device__ bool node_enter(Worker &W, Frame &f, int ply, int &value) {
+  W.nodes++;
+  f.key = search_key(f.pos, f.stm);
+  Move ttm = 0;
+  int ts, td, tb;
+  Move tm;
+  if (tt_probe(W.tt, W.tt_mask, f.key, ts, td, tb, tm)) {
+    if (td == f.depth) {
+      ttm = tm;
+      int s = from_tt(ts, ply);
+      if (ply > 0 && (tb == B_EXACT || (tb == B_LOWER && s >= f.beta) || (tb == B_UPPER && s <= f.alpha))) {
+        W.tthits++;
+        value = s;
+        return false;
+      }
+    }
+  }
+  const u64 bidx = (f.key >> 32) & W.busy_mask;
+  if (f.exclusive && f.depth >= kAbdadaMinDepth && ((volatile uint32_t *)W.busy)[bidx] > 0) {
+    value = kOnEval;
+    return false;
+  }
+  f.n = s_gen(f.pos, f.stm, f.moves);
+  if (f.n == 0) {
+    bool chk;
+    s_count(f.pos, f.stm, &chk);
+    value = chk ? -kSearchInf + ply : 0;
+    return false;
+  }
+  /* order once: insertion sort by score, best first */
+  const Move k0 = W.killer[ply][0], k1 = W.killer[ply][1];
+  for (int i = 0; i < f.n; i++) {
+    Move m = f.moves[i];
+    int s = order_score(m, f.stm, ttm, k0, k1, *W.T);
+    int j = i;
+    while (j > 0 && W.scores[j - 1] < s) {
+      W.scores[j] = W.scores[j - 1];
+      f.moves[j] = f.moves[j - 1];
+      j--;
+    }
+    W.scores[j] = s;
+    f.moves[j] = m;
+  }
+  f.busy = f.depth >= kAbdadaMinDepth;
+  if (f.busy) atomicAdd(&W.busy[bidx], 1u);
+  f.best = -kSearchInf - 1;
+  f.bestmove = 0;
+  f.alpha0 = f.alpha;
+  f.i = f.iter = f.searched = 0;
+  f.deferred = 0;
+  return true;
+}
+
+/* all moves searched or cut: store and return the value */
+__device__ __forceinline__ int node_finish(Worker &W, Frame &f, int ply) {
+  if (f.busy) atomicSub(&W.busy[(f.key >> 32) & W.busy_mask], 1u);
+  int bound = f.best <= f.alpha0 ? B_UPPER : (f.best >= f.beta ? B_LOWER : B_EXACT);
+  tt_store(W.tt, W.tt_mask, f.key, to_tt(f.best, ply), f.depth, bound, f.bestmove);
+  return f.best;
+}
+
+template <int TPB>
+__global__ void __launch_bounds__(TPB) k_search_pure(const uint64_t *__restrict__ boards, const uint8_t *__restrict__ stm,
+                                                     int N, int nworkers, int depth, TTEntry *tt, u64 tt_mask,
+                                                     uint32_t *busy, u64 busy_mask, uint32_t *done, SearchOut *out,
+                                                     unsigned long long budget, uint32_t *status) {
+  __shared__ EvalTables sT;
+  for (int i = threadIdx.x; i < (int)(sizeof(EvalTables) / 4); i += TPB)
+    ((uint32_t *)&sT)[i] = ((const uint32_t *)&kEvalDev)[i];
+  __syncthreads();
+  const long long t = (long long)blockIdx.x * TPB + threadIdx.x;
+  if (t >= (long long)N * nworkers) return;
+  const int p = (int)(t % N);
+
+  Frame F[kMaxSearchDepth + 1];
+  Worker W;
+  W.tt = tt;
+  W.tt_mask = tt_mask;
+  W.busy = busy;
+  W.busy_mask = busy_mask;
+  W.T = &sT;
+  W.nodes = W.tthits = 0;
+  for (int i = 0; i <= kMaxSearchDepth; i++) W.killer[i][0] = W.killer[i][1] = 0;
+
+  const uint64_t *b = boards + 7 * (size_t)p;
+  F[0].pos.b0 = b[0];
+  F[0].pos.p1 = b[1];
+  F[0].pos.p2 = b[2];
+  F[0].pos.p3 = b[3];
+  F[0].pos.cr = b[4];
+  F[0].stm = stm[p] & 1;
+  F[0].depth = depth;
+  F[0].alpha = -kSearchInf - 1;
+  F[0].beta = kSearchInf + 1;
+  F[0].exclusive = 0;
+  int v;
+  if (!node_enter(W, F[0], 0, v)) {
+    /* no legal move at the root: the game is over */
+    if (atomicCAS(&done[p], 0u, 1u) == 0u) {
+      out[p].score = v;
+      out[p].bestmove = 0;
+    }
+    atomicAdd(&out[p].nodes, W.nodes);
+    return;
+  }
+  int ply = 0;
+  unsigned long long steps = 0;
+  for (;;) {
+    if (++steps > budget) {
+      atomicOr(status, SST_BUDGET);
+      break;
+    }
+    if ((steps & 15) == 0 && ((volatile uint32_t *)done)[p]) break; /* another worker finished */
+    Frame &f = F[ply];
+    int val = 0;
+    bool deferred = false;
+    /* next move of this node: skip searched ones, and in the second pass
+     * everything that was not deferred */
+    while (f.i < f.n && ((f.moves[f.i] & kDone) || (f.iter == 1 && !(f.moves[f.i] & kDefer)))) f.i++;
+    if (f.i >= f.n) {
+      if (f.iter == 0 && f.deferred) {
+        f.iter = 1;
+        f.i = 0;
+        f.deferred = 0;
+        continue;
+      }
+      int r = node_finish(W, f, ply);
+      if (ply == 0) {
+        if (atomicCAS(&done[p], 0u, 1u) == 0u) {
+          out[p].score = r;
+          out[p].bestmove = f.bestmove;
+        }
+        break;
+      }
+      ply--;
+      val = -r;
+    } else {
+      const Move m = f.moves[f.i] & kMoveBits;
+      Pos c = f.pos;
+      play(c, m, false);
+      if (f.depth == 1) {
+        W.nodes++;
+        val = -leaf_value(c, f.stm ^ 1, ply + 1, W.T);
+      } else {
+        Frame &g = F[ply + 1];
+        g.pos = c;
+        g.stm = f.stm ^ 1;
+        g.depth = f.depth - 1;
+        g.alpha = -f.beta;
+        g.beta = -(f.alpha > f.best ? f.alpha : f.best);
+        g.exclusive = (f.iter == 0 && f.searched > 0);
+        int cv;
+        if (node_enter(W, g, ply + 1, cv)) {
+          ply++;
+          continue;
+        }
+        if (cv == kOnEval) deferred = true;
+        else val = -cv;
+      }
+    }
+    /* a child of F[ply] returned `val` (or was deferred) */
+    Frame &h = F[ply];
+    if (deferred) {
+      h.moves[h.i] |= kDefer;
+      h.deferred = 1;
+      h.i++;
+      continue;
+    }
+    const Move m = h.moves[h.i] & kMoveBits;
+    h.moves[h.i] = (h.moves[h.i] & kMoveBits) | kDone;
+    h.i++;
+    h.searched++;
+    if (val > h.best) {
+      h.best = val;
+      h.bestmove = m;
+    }
+    if (h.best > h.alpha) h.alpha = h.best;
+    if (h.best >= h.beta) {
+      if (!(m_pcpt(m) >> 1) && (m_pto(m) == m_pfrom(m)) && W.killer[ply][0] != m) {
+        W.killer[ply][1] = W.killer[ply][0];
+        W.killer[ply][0] = m;
+      }
+      h.i = h.n; /* cut: nothing else to search here */
+      h.deferred = 0;
+    }
+  }
+  atomicAdd(&out[p].nodes, W.nodes);
+  atomicAdd(&out[p].tthits, W.tthits);
+}
+
+__global__ void k_search_scatter(const SearchOut *out, int n, int32_t *scores, uint32_t *moves,
+                                 unsigned long long *nodes) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  if (scores) scores[i] = out[i].score;
+  if (moves) moves[i] = out[i].bestmove;
+  if (nodes) nodes[i] = out[i].nodes;
+}
+
+}  // namespace
+
+/* search buffers: outputs per position, the ABDADA busy table, the
+ * transposition table (zeta_init's tt1, else a 64 MiB table of our own) */
+static int search_buffers(int n) {
+  Context &c = ctx();
+  if (n > c.s_cap) {
+    cudaFree(c.s_out);
+    cudaFree(c.s_done);
+    c.s_out = nullptr;
+    c.s_done = nullptr;
+    c.s_cap = 0;
+    ZCHECK(cudaMalloc(&c.s_out, (size_t)n * sizeof(SearchOut)));
+    ZCHECK(cudaMalloc(&c.s_done, (size_t)n * sizeof(uint32_t)));
+    c.s_cap = n;
+  }
+  if (!c.s_busy) {
+    c.s_busy_entries = 1ull << 22;
+    ZCHECK(cudaMalloc(&c.s_busy, c.s_busy_entries * sizeof(uint32_t)));
+  }
+  if (!c.s_status) ZCHECK(cudaMalloc(&c.s_status, sizeof(uint32_t)));
+  if (!c.tt1 && !c.s_tt) {
+    c.s_tt_entries = 1ull << 22; /* 64 MiB of 16-byte entries */
+    ZCHECK(cudaMalloc(&c.s_tt, c.s_tt_entries * sizeof(TTEntry)));
+    ZCHECK(cudaMemset(c.s_tt, 0, c.s_tt_entries * sizeof(TTEntry)));
+  }
+  return ZETA_OK;
+}
+
+int search_tt_clear(cudaStream_t s) {
+  Context &c = ctx();
+  if (c.tt1) ZCHECK(cudaMemsetAsync(c.tt1, 0, c.tt1_entries * 16, s));
+  if (c.s_tt) ZCHECK(cudaMemsetAsync(c.s_tt, 0, c.s_tt_entries * sizeof(TTEntry), s));
+  return ZETA_OK;
+}
+
+int search_pure_launch(const uint64_t *d_boards, const uint8_t *d_stm, int n, int depth, int workers, int32_t *d_scores,
+                       uint32_t *d_moves, unsigned long long *d_nodes, cudaStream_t s) {
+  Context &c = ctx();
+  if (n <= 0 || workers <= 0 || depth < 1 || depth > kMaxSearchDepth - 1)
+    return set_error(ZETA_ERR_ARG, "search: need n > 0, workers > 0, depth 1..%d", kMaxSearchDepth - 1);
+  if ((long long)n * workers > (1ll << 31)) return set_error(ZETA_ERR_ARG, "search: too many workers");
+  int rc = search_buffers(n);
+  if (rc) return rc;
+  TTEntry *tt = (TTEntry *)(c.tt1 ? c.tt1 : c.s_tt);
+  u64 entries = c.tt1 ? c.tt1_entries : c.s_tt_entries;
+  ZCHECK(cudaMemsetAsync(c.s_out, 0, (size_t)n * sizeof(SearchOut), s));
+  ZCHECK(cudaMemsetAsync(c.s_done, 0, (size_t)n * sizeof(uint32_t), s));
+  ZCHECK(cudaMemsetAsync(c.s_busy, 0, c.s_busy_entries * sizeof(uint32_t), s));
+  ZCHECK(cudaMemsetAsync(c.s_status, 0, sizeof(uint32_t), s));
+  const long long threads = (long long)n * workers;
+  const int tpb = 128;
+  const unsigned long long budget = 1ull << 40;
+  ZCHECK(cudaEventRecord(c.ev[1], s));
+  k_search_pure<128><<<(unsigned)((threads + tpb - 1) / tpb), tpb, 0, s>>>(
+      d_boards, d_stm, n, workers, depth, tt, entries - 1, c.s_busy, c.s_busy_entries - 1, c.s_done,
+      (SearchOut *)c.s_out, budget, c.s_status);
+  ZCHECK(cudaGetLastError());
+  ZCHECK(cudaEventRecord(c.ev[2], s));
+  k_search_scatter<<<(n + 127) / 128, 128, 0, s>>>((const SearchOut *)c.s_out, n, d_scores, d_moves, d_nodes);
+  ZCHECK(cudaGetLastError());
+  uint32_t status = 0;
+  ZCHECK(cudaMemcpyAsync(&status, c.s_status, 4, cudaMemcpyDeviceToHost, s));
+  ZCHECK(cudaStreamSynchronize(s));
+  float ms = -1.f;
+  if (cudaEventElapsedTime(&ms, c.ev[1], c.ev[2]) != cudaSuccess) ms = -1.f;
+  (void)cudaGetLastError();
+  c.sstats.kernel_ms = ms;
+  if (status & SST_BUDGET) return set_error(ZETA_ERR_BUDGET, "search: a worker ran out of its node budget");
+  return ZETA_OK;
+}
+
+}  // namespace zeta
+
