@@ -290,6 +290,80 @@ def cpu_baseline_sample(boards, stm, depth, budget_s: float = 12.0):
                       f"first {k} workload positions at depth 3, {total_leaves} leaves in {total_s:.1f}s"}
 
 
+def run_search(args):
+    """Batched fixed-depth pure search: 1024 seeded playout positions (20-40
+    plies, >= 20 pieces) at depth 7, ABDADA workers per position, 1 GiB
+    transposition table cleared at the start of every step (part of the
+    timed work).  Metric: positions per second."""
+    import torch
+    import zeta_gb300 as z
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    z.init(local, 1024, 0)
+    w = dict(z.WORKLOADS["search_batch"])
+    n = args.n or w["n"]
+    boards, stm, _ = z.make_positions(w["seed"] + 0x1000003 * rank, n, w["min_plies"], w["max_plies"],
+                                      w["min_pieces"], 0, 0)
+    depth = args.depth or 7
+    dev = torch.device("cuda", local)
+    d_b = torch.from_numpy(boards.view(np.int64)).to(dev)
+    d_s = torch.from_numpy(stm).to(dev)
+    d_sc = torch.zeros(n, dtype=torch.int32, device=dev)
+    d_mv = torch.zeros(n, dtype=torch.int32, device=dev)
+    d_nd = torch.zeros(n, dtype=torch.int64, device=dev)
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
+    # (workers per position, helper cap): helpers let finished workers join
+    # unfinished positions up to `cap` workers each (0 = no helping)
+    workers_list = ([(args.workers, args.helpers)] if args.workers else
+                    [(32, 0), (64, 0), (16, 48), (32, 64), (32, 96)])
+    results = {}
+    ref_scores = None
+    for W, cap in workers_list:
+        z.search_set_helpers(cap)
+        for _ in range(1 if len(workers_list) > 1 else args.warmup):
+            z.tt_clear()
+            z.search_batch_device(d_b.data_ptr(), d_s.data_ptr(), n, depth, W, d_sc.data_ptr(), d_mv.data_ptr(),
+                                  d_nd.data_ptr(), stream.cuda_stream)
+        steps = 1 if len(workers_list) > 1 else args.steps
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        nodes = 0
+        kms = []
+        for _ in range(steps):
+            z.tt_clear()
+            z.search_batch_device(d_b.data_ptr(), d_s.data_ptr(), n, depth, W, d_sc.data_ptr(), d_mv.data_ptr(),
+                                  d_nd.data_ptr(), stream.cuda_stream)
+            kms.append(z.search_last_ms())
+            nodes += int(d_nd.sum().item())
+        torch.cuda.synchronize()
+        dt = (time.perf_counter() - t0) / steps
+        sc = d_sc.cpu().numpy().copy()
+        if ref_scores is None:
+            ref_scores = sc
+        if not np.array_equal(sc, ref_scores):
+            raise SystemExit(f"root scores changed with {W} workers")
+        key = f"{W}/{cap}"
+        results[key] = {"positions_per_s": n / dt, "ms_per_step": dt * 1e3, "kernel_ms": sum(kms) / len(kms),
+                        "nodes_per_s": nodes / steps / dt, "nodes_per_step": nodes // steps}
+        print(json.dumps({"workers/helper_cap": key, **results[key]}), file=sys.stderr, flush=True)
+    best_w = max(results, key=lambda k: results[k]["positions_per_s"])
+    r = results[best_w]
+    if rank == 0:
+        print(json.dumps({
+            "metric": "batched search positions/s (fixed depth 7, root score = plain negamax)",
+            "value": round(r["positions_per_s"], 2), "unit": "positions/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(r["ms_per_step"], 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded random playouts)",
+            "config": {"workload": f"search_batch: {n} playouts of 20-40 plies, >=20 pieces, depth {depth}",
+                       "workers_per_position/helper_cap": best_w,
+                       "tt": "1 GiB, 16-byte entries, cleared every step"},
+            "nodes_per_s": round(r["nodes_per_s"], 1), "nodes_per_step": r["nodes_per_step"],
+            "sweep": {str(k): round(v["positions_per_s"], 2) for k, v in results.items()},
+        }), flush=True)
+    z.release()
+
+
 def run_reference(args):
     world, rank, _ = dist_env()
     if rank != 0:
@@ -338,10 +412,16 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--n", type=int, default=0, help="positions per GPU (default: the workload's 4096)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the timed CPU baseline (profiling runs)")
+    ap.add_argument("--workload", choices=["perft_batch", "search_batch"], default="perft_batch")
+    ap.add_argument("--depth", type=int, default=0, help="search depth (search_batch; default 7)")
+    ap.add_argument("--workers", type=int, default=0, help="ABDADA workers per position (0 = sweep)")
+    ap.add_argument("--helpers", type=int, default=0, help="helper cap: max workers per position (0 = none)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    if args.impl == "reference":
+    if args.workload == "search_batch" and args.impl == "ours":
+        run_search(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

@@ -129,10 +129,29 @@ int zeta_search_batch(const uint64_t *boards, const uint8_t *stm, int n, int dep
 /* same with device buffers, on `stream` (NULL = the library's stream) */
 int zeta_search_batch_device(const uint64_t *d_boards, const uint8_t *d_stm, int n, int depth, int workers,
                              int32_t *d_scores, uint32_t *d_bestmoves, uint64_t *d_nodes, void *stream);
+/* One position to `depth` (cl_run_alphabeta, src/clrun.c:675-974, with
+ * the read-back of src/clrun.c:1150-1266): pv[0] = root score, pv[1] =
+ * best move; counters[1] = visited nodes.  ply_init, hash_history and
+ * max_nodes carry the reference's arguments (game ply, repetition history
+ * of MAXGAMEPLY hashes, node budget); the fixed-depth search does not
+ * use them. */
+int zeta_search(const uint64_t board[7], int stm, int depth, int ply_init, const uint64_t *hash_history,
+                uint64_t max_nodes, uint32_t pv[64], uint64_t counters[64]);
+/* Workers that finish their own position help unfinished ones, up to this
+ * many workers per position (0, the default: no helping). */
+int zeta_search_set_helpers(int max_workers_per_position);
 /* zero the transposition tables (as a new game does, src/xboard.c:159-199) */
 int zeta_tt_clear(void);
 /* device time of the last search kernel, ms */
 int zeta_search_last_ms(float *kernel_ms);
+
+/* ------------------------------------------------------------------ */
+/* Tensor-core matrix product used by the move-ordering network (test and
+ * tooling entry; no counterpart in the reference): C[M x N] fp32 =
+ * A[M x K] . B[N x K]^T, operands K-major BF16 (fp8 == 0) or FP8 E4M3
+ * (fp8 != 0), device buffers, K a multiple of 64 (BF16) or 128 (FP8), N a
+ * multiple of 16.  tcgen05.mma with FP32 accumulation in tensor memory. */
+int zeta_gemm_tc(const void *d_A, const void *d_B, float *d_C, int M, int N, int K, int fp8, void *stream);
 
 /* ------------------------------------------------------------------ */
 /* Seeded synthetic positions generated on the device (the benchmark

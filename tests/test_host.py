@@ -1,0 +1,89 @@
+"""The C host: its board layer against the oracle (CPU), and the zeta
+binary's selftest and xboard session on the GPU."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import oracle_lib as ol
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HOST = os.path.join(ROOT, "zeta_gb300", "host")
+ZETA = os.path.join(ROOT, "zeta_gb300", "_build", "zeta")
+
+HARNESS = r"""
+#include <stdio.h>
+#include "board.h"
+int main(void) {
+  char fen[512];
+  while (fgets(fen, sizeof fen, stdin)) {
+    Bitboard b[7]; int stm, full;
+    int ok = board_setfen(b, &stm, &full, fen);
+    char out[256]; board_getfen(b, stm, full, out, sizeof out);
+    printf("%d %d", ok, stm);
+    for (int i = 0; i < 7; i++) printf(" %llx", (unsigned long long)b[i]);
+    printf(" %llx|%s\n", (unsigned long long)board_hash(b, stm), out);
+  }
+  return 0;
+}
+"""
+
+
+@pytest.fixture(scope="module")
+def harness(tmp_path_factory):
+    d = tmp_path_factory.mktemp("host")
+    src = d / "h.c"
+    src.write_text(HARNESS)
+    exe = d / "h"
+    subprocess.run(["gcc", "-O1", "-std=gnu11", "-I", HOST, "-o", str(exe), str(src), os.path.join(HOST, "board.c")],
+                   check=True)
+    return str(exe)
+
+
+FENS = ["rnbqkbnr/pppppppp/8/8/8/8/PPPPPPPP/RNBQKBNR w KQkq - 0 1",
+        "r3k2r/p1ppqpb1/bn2pnp1/3PN3/1p2P3/2N2Q1p/PPPBBPPP/R3K2R w KQkq - 0 1",
+        "8/2p5/3p4/KP5r/1R3p1k/8/4P1P1/8 w - - 0 1",
+        "r4rk1/1pp1qppp/p1np1n2/2b1p1B1/2B1P1b1/P1NP1N2/1PP1QPPP/R4RK1 w - - 0 10",
+        "rnbqkbnr/ppp1pppp/8/3pP3/8/8/PPPP1PPP/RNBQKBNR b Kq d6 4 3",
+        "4k3/8/8/8/8/8/8/4K2R w K - 0 1"]
+
+
+def test_host_board_layer_matches_oracle(harness):
+    out = subprocess.run([harness], input="\n".join(FENS) + "\n", capture_output=True, text=True, check=True).stdout
+    for fen, line in zip(FENS, out.strip().splitlines()):
+        head, fen_out = line.split("|")
+        f = head.split()
+        b, stm = ol.setboard(fen)
+        assert int(f[0]) == 1 and int(f[1]) == stm
+        assert [int(x, 16) for x in f[2:9]] == [int(x) for x in b]
+        assert int(f[9], 16) == ol.computehash(b, stm)
+        # the FEN the host writes sets the same board again
+        b2, s2 = ol.setboard(fen_out)
+        assert [int(x) for x in b2[:4]] == [int(x) for x in b[:4]] and s2 == stm
+
+
+def test_zeta_binary_help_runs_without_gpu():
+    if not os.path.exists(ZETA):
+        pytest.skip("host binary not built")
+    r = subprocess.run([ZETA, "--help"], capture_output=True, text=True, timeout=30)
+    assert r.returncode == 0 and "--selftest" in r.stdout
+
+
+@pytest.mark.gpu
+def test_zeta_selftest_passes_all_14():
+    r = subprocess.run([ZETA, "-s"], capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "passed 14 from 14" in r.stdout
+
+
+@pytest.mark.gpu
+def test_zeta_xboard_session_plays_a_legal_move():
+    session = "xboard\nprotover 2\nnew\nsd 4\nusermove e2e4\nquit\n"
+    r = subprocess.run([ZETA], input=session, capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert r.returncode == 0, r.stderr
+    moves = [l.split()[1] for l in r.stdout.splitlines() if l.startswith("move ")]
+    assert len(moves) == 1
+    b, s = ol.setboard("rnbqkbnr/pppppppp/8/8/4P3/8/PPPP1PPP/RNBQKBNR b KQkq - 0 1")
+    legal = {ol.move2can(m) for m in ol.genmoves(b, s)}
+    assert moves[0] in legal

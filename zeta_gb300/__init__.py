@@ -87,7 +87,22 @@ SIGNATURES = {
     "zeta_search_batch_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
                                                 ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                                 ctypes.c_void_p]),
+    "zeta_gemm_tc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                                    ctypes.c_int, ctypes.c_int, ctypes.c_void_p]),
+    "zeta_mlp_init": (ctypes.c_int, [ctypes.c_uint64]),
+    "zeta_mlp_param_count": (ctypes.c_int, []),
+    "zeta_mlp_get_params": (ctypes.c_int, [ctypes.POINTER(ctypes.c_float)]),
+    "zeta_mlp_set_params": (ctypes.c_int, [ctypes.POINTER(ctypes.c_float)]),
+    "zeta_mlp_grads": (ctypes.c_int, [_u64p, _u8p, _u32p, ctypes.c_int, ctypes.POINTER(ctypes.c_float),
+                                      ctypes.POINTER(ctypes.c_float)]),
+    "zeta_mlp_train": (ctypes.c_int, [_u64p, _u8p, _u32p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_float,
+                                      ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]),
+    "zeta_mlp_scores": (ctypes.c_int, [_u64p, _u8p, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_float), _u8p,
+                                       _i32p]),
+    "zeta_search": (ctypes.c_int, [_u64p, ctypes.c_int, ctypes.c_int, ctypes.c_int, _u64p, ctypes.c_uint64, _u32p,
+                                   _u64p]),
     "zeta_tt_clear": (ctypes.c_int, []),
+    "zeta_search_set_helpers": (ctypes.c_int, [ctypes.c_int]),
     "zeta_search_last_ms": (ctypes.c_int, [ctypes.POINTER(ctypes.c_float)]),
     "zeta_genmoves_batch": (ctypes.c_int, [_u64p, _u8p, ctypes.c_int, ctypes.c_int, _u32p, _i32p]),
 }
@@ -208,6 +223,82 @@ def search_batch_device(d_boards: int, d_stm: int, n: int, depth: int, workers: 
                         d_nodes: int, stream: int = 0) -> None:
     _check(load_library().zeta_search_batch_device(d_boards, d_stm, n, depth, workers, d_scores, d_moves, d_nodes,
                                                    stream or None))
+
+
+def search_set_helpers(max_workers_per_position: int) -> None:
+    _check(load_library().zeta_search_set_helpers(max_workers_per_position))
+
+
+def gemm_tc(d_a: int, d_b: int, d_c: int, m: int, n: int, k: int, fp8: bool = False, stream: int = 0) -> None:
+    """C[m x n] fp32 = A[m x k] . B[n x k]^T on the tcgen05 tensor cores (device pointers)."""
+    _check(load_library().zeta_gemm_tc(d_a, d_b, d_c, m, n, k, int(fp8), stream or None))
+
+
+_f32p = ctypes.POINTER(ctypes.c_float)
+
+# layout of the network's flat FP32 parameter vector
+MLP_SHAPES = [("W1", (512, 768)), ("b1", (512,)), ("W2", (256, 512)), ("b2", (256,)), ("W3", (128, 256)),
+              ("b3", (128,)), ("Ef", (64, 64)), ("Et", (64, 64))]
+
+
+def mlp_init(seed: int = 1) -> None:
+    _check(load_library().zeta_mlp_init(seed))
+
+
+def mlp_get_params() -> np.ndarray:
+    p = np.zeros(load_library().zeta_mlp_param_count(), dtype=np.float32)
+    _check(load_library().zeta_mlp_get_params(_ptr(p, _f32p)))
+    return p
+
+
+def mlp_set_params(p: np.ndarray) -> None:
+    p = np.ascontiguousarray(p, dtype=np.float32)
+    _check(load_library().zeta_mlp_set_params(_ptr(p, _f32p)))
+
+
+def mlp_unflatten(p: np.ndarray) -> dict:
+    out, off = {}, 0
+    for name, shape in MLP_SHAPES:
+        n = int(np.prod(shape))
+        out[name] = p[off:off + n].reshape(shape)
+        off += n
+    return out
+
+
+def mlp_grads(boards, stm, targets):
+    b = np.ascontiguousarray(boards, dtype=np.uint64).reshape(-1, 7)
+    s = np.ascontiguousarray(stm, dtype=np.uint8)
+    t = np.ascontiguousarray(targets, dtype=np.uint32)
+    g = np.zeros(load_library().zeta_mlp_param_count(), dtype=np.float32)
+    loss = ctypes.c_float()
+    _check(load_library().zeta_mlp_grads(_ptr(b, _u64p), _ptr(s, _u8p), _ptr(t, _u32p), b.shape[0], _ptr(g, _f32p),
+                                         ctypes.byref(loss)))
+    return g, loss.value
+
+
+def mlp_train(boards, stm, targets, epochs: int = 1, batch: int = 4096, lr: float = 1e-3):
+    b = np.ascontiguousarray(boards, dtype=np.uint64).reshape(-1, 7)
+    s = np.ascontiguousarray(stm, dtype=np.uint8)
+    t = np.ascontiguousarray(targets, dtype=np.uint32)
+    loss = np.zeros(epochs, dtype=np.float32)
+    acc = np.zeros(epochs, dtype=np.float32)
+    _check(load_library().zeta_mlp_train(_ptr(b, _u64p), _ptr(s, _u8p), _ptr(t, _u32p), b.shape[0], epochs, batch,
+                                         lr, _ptr(loss, _f32p), _ptr(acc, _f32p)))
+    return loss, acc
+
+
+def mlp_scores(boards, stm, fp8: bool = False):
+    """(scores n x 218, counts n, best index n) of every legal move, in the
+    engine's move-generation order."""
+    b = np.ascontiguousarray(boards, dtype=np.uint64).reshape(-1, 7)
+    s = np.ascontiguousarray(stm, dtype=np.uint8)
+    n = b.shape[0]
+    sc = np.zeros((n, 218), dtype=np.float32)
+    nm = np.zeros(n, dtype=np.uint8)
+    best = np.zeros(n, dtype=np.int32)
+    _check(load_library().zeta_mlp_scores(_ptr(b, _u64p), _ptr(s, _u8p), n, int(fp8), _ptr(sc, _f32p), _ptr(nm, _u8p),
+                                          _ptr(best, _i32p)))
+    return sc, nm, best
 
 
 def tt_clear() -> None:

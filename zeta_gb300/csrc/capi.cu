@@ -116,6 +116,7 @@ int zeta_release(void) {
   Context &c = g_ctx;
   if (!c.ready) return ZETA_OK;
   if (c.graph) cudaGraphExecDestroy(c.graph);
+  mlp_free();
   cudaFree(c.lvl[0]);
   cudaFree(c.lvl[1]);
   cudaFree(c.fin);
@@ -296,6 +297,43 @@ int zeta_search_batch(const uint64_t *boards, const uint8_t *stm, int n, int dep
   cudaFree(dn);
   if (e != cudaSuccess) return cuda_fail(e, "zeta_search_batch");
   return rc;
+}
+
+/* One position, one launch (cl_run_alphabeta, src/clrun.c:675-974): the
+ * batched search with `workers` ABDADA workers on the single position.
+ * pv[0] = score, pv[1] = best move (the rest 0); counters[1] = nodes,
+ * counters[4] = transposition-table score hits (src/search.c:114-121
+ * reads these slots). */
+int zeta_search(const uint64_t board[7], int stm, int depth, int ply_init, const uint64_t *hash_history,
+                uint64_t max_nodes, uint32_t pv[64], uint64_t counters[64]) {
+  (void)ply_init;
+  (void)hash_history;
+  (void)max_nodes;
+  int rc = require_ready();
+  if (rc) return rc;
+  if (!board || depth < 1) return set_error(ZETA_ERR_ARG, "bad search arguments");
+  uint8_t s = (uint8_t)(stm & 1);
+  int32_t score = 0;
+  uint32_t move = 0;
+  uint64_t nodes = 0;
+  rc = zeta_search_batch(board, &s, 1, depth, 64, &score, &move, &nodes);
+  if (rc) return rc;
+  if (pv) {
+    memset(pv, 0, 64 * sizeof(uint32_t));
+    pv[0] = (uint32_t)score;
+    pv[1] = move;
+  }
+  if (counters) {
+    memset(counters, 0, 64 * sizeof(uint64_t));
+    counters[1] = nodes;
+  }
+  return ZETA_OK;
+}
+
+int zeta_search_set_helpers(int max_workers_per_position) {
+  if (max_workers_per_position < 0) return set_error(ZETA_ERR_ARG, "negative helper cap");
+  g_ctx.s_helpers_cap = max_workers_per_position;
+  return ZETA_OK;
 }
 
 int zeta_tt_clear(void) {

@@ -80,6 +80,7 @@ struct Context {
   zeta_perft_config g_cfg{};
 
   /* transposition tables (search) */
+  void *mlp = nullptr; /* move-ordering network state (mlp.cu) */
   void *tt1 = nullptr, *tt2 = nullptr;
   uint64_t tt1_entries = 0, tt2_entries = 0;
 
@@ -90,6 +91,7 @@ struct Context {
   uint32_t *s_busy = nullptr; /* ABDADA busy table */
   uint64_t s_busy_entries = 0;
   uint32_t *s_status = nullptr;
+  int s_helpers_cap = 0;      /* max workers per position once helpers join; 0 = no helpers */
   void *s_tt = nullptr;       /* used when zeta_init made no table */
   uint64_t s_tt_entries = 0;
   struct {
@@ -118,6 +120,8 @@ int int_peak(double *tops);
 int search_pure_launch(const uint64_t *d_boards, const uint8_t *d_stm, int n, int depth, int workers, int32_t *d_scores,
                        uint32_t *d_moves, unsigned long long *d_nodes, cudaStream_t s);
 int search_tt_clear(cudaStream_t s);
+/* mlp.cu */
+void mlp_free();
 int genmoves_launch(const uint64_t *d_boards, const uint8_t *d_stm, int n, int qs, uint32_t *d_moves,
                     int32_t *d_counts, cudaStream_t stream);
 

@@ -1,0 +1,762 @@
+/*
+ * mlp.cu -- the learned move-ordering network on Blackwell tensor cores.
+ *
+ * Network (the project's addition; the reference orders moves by hand,
+ * zeta.cl:2039-2110): 768 one-hot inputs (12 piece kinds x 64 squares,
+ * from the side to move, board mirrored for black) -> 512 ReLU -> 256 ReLU
+ * -> 128 = (q_from, q_to), and a move's score is
+ * q_from . E_from[from] + q_to . E_to[to] with learned 64-wide square
+ * embeddings.  Training minimises the softmax cross-entropy of the legal
+ * moves against the best move of a plain search.
+ *
+ * Every matrix product -- forward, input gradients, weight gradients -- is
+ * one kernel, k_gemm: C[M x N] = A[M x K] . B[N x K]^T with both operands
+ * K-major BF16 (or FP8 E4M3 for inference), FP32 accumulation in tensor
+ * memory.  A CTA owns a 128-row by BN-column output tile: its threads
+ * stage 64-element (BF16) or 128-element (FP8) K slices of A and B into
+ * 128-byte-swizzled shared memory, one thread issues the tcgen05.mma
+ * instructions and commits them to an mbarrier, and after the K loop the
+ * four warps read their 32 accumulator lanes back with tcgen05.ld and
+ * apply the epilogue (bias, ReLU, FP32 / BF16 / transposed BF16 stores).
+ * Every wait is bounded; a timeout sets an error word and the kernel
+ * still frees its tensor memory.
+ */
+#include <cuda_bf16.h>
+#include <cuda_fp8.h>
+
+#include <cmath>
+#include <cstdio>
+#include <vector>
+
+#include "context.cuh"
+#include "tc.cuh"
+
+namespace zeta {
+
+namespace {
+
+typedef __nv_bfloat16 bf16;
+constexpr uint32_t kWaitTries = 1u << 22;
+constexpr uint32_t MST_TIMEOUT = 1u;
+
+struct GemmArgs {
+  const void *A;      /* M x K, K-major */
+  const void *B;      /* N x K, K-major */
+  int M, N, K;
+  const float *bias;  /* N, or null */
+  int relu;
+  float *Cf;          /* M x N fp32 (ldc = N), or null */
+  bf16 *Cb;           /* M x N bf16, or null */
+  bf16 *Ct;           /* N x M bf16 (transposed), or null */
+  float scale;        /* multiplies the accumulator (FP8 dequantisation) */
+  uint32_t *err;
+  const bf16 *mask;   /* M x N: zero where mask <= 0 (ReLU derivative), or null */
+  const unsigned *amaxA, *amaxB; /* FP8: per-tensor max |x| (float bits); scale *= amaxA*amaxB/448^2 */
+};
+
+/* BN: output columns per CTA (64, 128 or 256); FP8: operands are e4m3 */
+template <int BN, bool FP8>
+__global__ void __launch_bounds__(128) k_gemm(GemmArgs g) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t *base = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint8_t *sA = base;           /* 128 rows x 128 bytes */
+  uint8_t *sB = base + 16384;   /* BN rows x 128 bytes */
+  __shared__ uint64_t bar;
+  __shared__ uint32_t s_taddr;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int m0 = blockIdx.x * 128, n0 = blockIdx.y * BN;
+  constexpr int EK = FP8 ? 128 : 64;           /* K elements per 128-byte row */
+  constexpr int ESZ = FP8 ? 1 : 2;             /* bytes per element */
+  constexpr uint32_t IDESC = FP8 ? tc::idesc_f8(128, BN) : tc::idesc_f16(128, BN, 1);
+
+  if (warp == 0) tc::tmem_alloc(&s_taddr, BN);
+  if (tid == 0) tc::mbar_init(&bar, 1);
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t taddr = s_taddr;
+  const uint8_t *Ag = (const uint8_t *)g.A, *Bg = (const uint8_t *)g.B;
+  const size_t rowbytes = (size_t)g.K * ESZ;
+  uint32_t phase = 0;
+  int ok = 1;
+  for (int k0 = 0; k0 < g.K; k0 += EK) {
+    for (int i = tid; i < 128 * 8; i += 128) {
+      const int r = i >> 3, c = i & 7;
+      uint4 v = make_uint4(0, 0, 0, 0);
+      if (m0 + r < g.M) v = *(const uint4 *)(Ag + (size_t)(m0 + r) * rowbytes + (size_t)k0 * ESZ + c * 16);
+      *(uint4 *)(sA + tc::sw128_offset(r, c)) = v;
+    }
+    for (int i = tid; i < BN * 8; i += 128) {
+      const int r = i >> 3, c = i & 7;
+      uint4 v = make_uint4(0, 0, 0, 0);
+      if (n0 + r < g.N) v = *(const uint4 *)(Bg + (size_t)(n0 + r) * rowbytes + (size_t)k0 * ESZ + c * 16);
+      *(uint4 *)(sB + tc::sw128_offset(r, c)) = v;
+    }
+    tc::fence_async_smem();
+    __syncthreads();
+    if (tid == 0) {
+      tc::fence_after_sync();
+      const uint32_t a0 = tc::smem_u32(sA), b0 = tc::smem_u32(sB);
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        const uint64_t ad = tc::smem_desc_sw128(a0 + 32 * j), bd = tc::smem_desc_sw128(b0 + 32 * j);
+        if (FP8) tc::mma_f8(taddr, ad, bd, IDESC, (k0 > 0 || j > 0) ? 1u : 0u);
+        else tc::mma_f16(taddr, ad, bd, IDESC, (k0 > 0 || j > 0) ? 1u : 0u);
+      }
+      tc::mma_commit(&bar);
+    }
+    /* the tiles may be overwritten only when the tensor cores are done */
+    ok &= tc::mbar_wait(&bar, phase, kWaitTries) ? 1 : 0;
+    phase ^= 1;
+    ok = __syncthreads_and(ok);
+    tc::fence_after_sync();
+    if (!ok) break;
+  }
+  if (ok) {
+    if (g.amaxA && g.amaxB)
+      g.scale *= (__uint_as_float(*g.amaxA) / 448.f) * (__uint_as_float(*g.amaxB) / 448.f);
+    const int row = m0 + warp * 32 + lane;
+#pragma unroll 1
+    for (int c0 = 0; c0 < BN; c0 += 16) {
+      float v[16];
+      tc::tmem_ld16(taddr + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+      if (row < g.M) {
+#pragma unroll
+        for (int j = 0; j < 16; j++) {
+          const int col = n0 + c0 + j;
+          if (col >= g.N) continue;
+          float x = v[j] * g.scale;
+          if (g.bias) x += g.bias[col];
+          if (g.relu) x = fmaxf(x, 0.f);
+          if (g.mask && !(__bfloat162float(g.mask[(size_t)row * g.N + col]) > 0.f)) x = 0.f;
+          if (g.Cf) g.Cf[(size_t)row * g.N + col] = x;
+          if (g.Cb) g.Cb[(size_t)row * g.N + col] = __float2bfloat16(x);
+          if (g.Ct) g.Ct[(size_t)col * g.M + row] = __float2bfloat16(x);
+        }
+      }
+    }
+  } else {
+    if (tid == 0) atomicOr(g.err, MST_TIMEOUT);
+    /* let the tensor cores drain (bounded) before the memory goes away */
+    tc::mbar_wait(&bar, phase ^ 1, kWaitTries);
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tc::tmem_free(taddr, BN);
+}
+
+constexpr size_t gemm_smem(int BN) { return 1024 + 16384 + (size_t)BN * 128; }
+
+}  // namespace
+
+/* C = A . B^T (+bias, relu) on the tensor cores; operands K-major, K a
+ * multiple of 64 (BF16) or 128 (FP8), N a multiple of 16. */
+int gemm_launch(const GemmArgs &g, bool fp8, cudaStream_t s) {
+  if (g.M <= 0 || g.N <= 0 || g.K <= 0 || (g.K % (fp8 ? 128 : 64)) || (g.N % 16))
+    return set_error(ZETA_ERR_ARG, "gemm: M %d N %d K %d not supported", g.M, g.N, g.K);
+  const int BN = g.N >= 256 ? 256 : (g.N > 64 ? 128 : 64);
+  dim3 grid((g.M + 127) / 128, (g.N + BN - 1) / BN);
+  const size_t sm = gemm_smem(BN);
+  /* at most two CTAs per SM: their tensor memory (<= 256 columns each)
+   * always fits the SM's 512 columns, so no allocation ever waits */
+  const size_t sm_req = sm < 80 * 1024 ? 80 * 1024 : sm;
+#define ZETA_GEMM_CASE(BNV)                                                                              \
+  if (BN == BNV) {                                                                                       \
+    auto k = fp8 ? k_gemm<BNV, true> : k_gemm<BNV, false>;                                               \
+    ZCHECK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_req));            \
+    k<<<grid, 128, sm_req, s>>>(g);                                                                      \
+  }
+  ZETA_GEMM_CASE(64)
+  ZETA_GEMM_CASE(128)
+  ZETA_GEMM_CASE(256)
+#undef ZETA_GEMM_CASE
+  ZCHECK(cudaGetLastError());
+  return ZETA_OK;
+}
+
+}  // namespace zeta
+
+using namespace zeta;
+
+/* Test and tooling entry: C[M x N] (fp32) = A[M x K] . B[N x K]^T with
+ * device buffers (bf16, or e4m3 when fp8 != 0).  Returns ZETA_ERR_BUDGET
+ * when a tensor-core wait timed out. */
+extern "C" int zeta_gemm_tc(const void *d_A, const void *d_B, float *d_C, int M, int N, int K, int fp8, void *stream) {
+  if (!d_A || !d_B || !d_C) return set_error(ZETA_ERR_ARG, "null buffer");
+  uint32_t *d_err = nullptr;
+  ZCHECK(cudaMalloc(&d_err, 4));
+  cudaStream_t s = (cudaStream_t)stream;
+  ZCHECK(cudaMemsetAsync(d_err, 0, 4, s));
+  GemmArgs g{d_A, d_B, M, N, K, nullptr, 0, d_C, nullptr, nullptr, 1.f, d_err, nullptr, nullptr, nullptr};
+  int rc = gemm_launch(g, fp8 != 0, s);
+  uint32_t err = 0;
+  if (rc == ZETA_OK) {
+    cudaError_t e = cudaMemcpyAsync(&err, d_err, 4, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) rc = cuda_fail(e, "zeta_gemm_tc");
+  }
+  cudaFree(d_err);
+  if (rc) return rc;
+  if (err) return set_error(ZETA_ERR_BUDGET, "gemm: tensor-core wait timed out");
+  return ZETA_OK;
+}
+
+/* ================================================================== */
+/* The network around the GEMMs                                        */
+/* ================================================================== */
+namespace zeta {
+namespace {
+
+constexpr int kIn = 768, kH1 = 512, kH2 = 256, kOut = 128, kEmb = 64;
+/* one flat FP32 parameter vector */
+constexpr size_t OFF_W1 = 0, OFF_B1 = OFF_W1 + (size_t)kH1 * kIn, OFF_W2 = OFF_B1 + kH1,
+                 OFF_B2 = OFF_W2 + (size_t)kH2 * kH1, OFF_W3 = OFF_B2 + kH2, OFF_B3 = OFF_W3 + (size_t)kOut * kH2,
+                 OFF_EF = OFF_B3 + kOut, OFF_ET = OFF_EF + (size_t)64 * kEmb, NPARAM = OFF_ET + (size_t)64 * kEmb;
+constexpr int kMaxLegal = 218;
+
+/* Input features from the side to move: plane = own/opponent x piece type,
+ * square mirrored (sq ^ 56) when black is to move.  Legal moves as
+ * (from, to) in the same frame; `target_idx` = index of the target move
+ * in that list (-1 when absent or no target given). */
+__global__ void k_features(const uint64_t *__restrict__ boards, const uint8_t *__restrict__ stm, const Move *targets,
+                           int n, int rows, bf16 *X, bf16 *Xt, uint16_t *moves, uint8_t *nmoves, int16_t *tidx) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= rows) return;
+  if (i >= n) { /* padding row: no features, no moves */
+    nmoves[i] = 0;
+    tidx[i] = -1;
+    return;
+  }
+  const uint64_t *b = boards + 7 * (size_t)i;
+  Pos p;
+  p.b0 = b[0];
+  p.p1 = b[1];
+  p.p2 = b[2];
+  p.p3 = b[3];
+  p.cr = b[4];
+  const int s = stm[i] & 1;
+  const int flip = s ? 56 : 0;
+  u64 occ = p.p1 | p.p2 | p.p3;
+  const bf16 one = __float2bfloat16(1.f);
+  while (occ) {
+    int sq = ctz(occ);
+    occ &= occ - 1;
+    int pc = piece_at(p, sq);
+    int plane = ((pc & 1) != s ? 6 : 0) + (pc >> 1) - 1;
+    int f = plane * 64 + (sq ^ flip);
+    X[(size_t)i * kIn + f] = one;
+    Xt[(size_t)f * rows + i] = one;
+  }
+  Move list[256];
+  int k = gen_legal(p, s, false, list);
+  int t = -1;
+  const Move target = targets ? (targets[i] & 0x3FFFFFFFu) : 0u;
+  for (int j = 0; j < k; j++) {
+    Move m = list[j];
+    moves[(size_t)i * kMaxLegal + j] = (uint16_t)((m_from(m) ^ flip) | ((m_to(m) ^ flip) << 6));
+    if (targets && m == target) t = j;
+  }
+  nmoves[i] = (uint8_t)k;
+  tidx[i] = (int16_t)t;
+}
+
+/* Softmax cross-entropy of the legal moves; one warp per position.
+ * logit(m) = q_from . Ef[from] + q_to . Et[to].  Writes dQ (and its
+ * transpose) scaled by 1/count, accumulates dEf / dEt, the loss and the
+ * number of positions whose best-scored move is the target.  With
+ * train == 0 it only writes the logits of the moves (scores). */
+__global__ void k_head(const float *__restrict__ Q, const float *__restrict__ params, const uint16_t *__restrict__ moves,
+                       const uint8_t *__restrict__ nmoves, const int16_t *__restrict__ tidx, int rows, float inv_count,
+                       int train, bf16 *dQ, bf16 *dQt, float *grads, float *loss, unsigned *correct, float *scores) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (warp >= rows) return;
+  const int i = warp;
+  const float *Ef = params + OFF_EF, *Et = params + OFF_ET;
+  const float qf0 = Q[(size_t)i * kOut + 2 * lane], qf1 = Q[(size_t)i * kOut + 2 * lane + 1];
+  const float qt0 = Q[(size_t)i * kOut + 64 + 2 * lane], qt1 = Q[(size_t)i * kOut + 64 + 2 * lane + 1];
+  const int k = nmoves[i];
+  const int t = tidx[i];
+  /* pass 1: logits (kept in lane j%32, slot j/32) and their maximum */
+  float mylog[7];
+  float mx = -1e30f;
+  int arg = -1;
+  for (int j = 0; j < k; j++) {
+    const uint16_t mv = moves[(size_t)i * kMaxLegal + j];
+    const int f = mv & 63, to = mv >> 6;
+    float x = qf0 * Ef[f * 64 + 2 * lane] + qf1 * Ef[f * 64 + 2 * lane + 1] + qt0 * Et[to * 64 + 2 * lane] +
+              qt1 * Et[to * 64 + 2 * lane + 1];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xFFFFFFFFu, x, o);
+    if ((j & 31) == lane) mylog[j >> 5] = x;
+    if (x > mx) {
+      mx = x;
+      arg = j;
+    }
+    if (scores) scores[(size_t)i * kMaxLegal + j] = x;
+  }
+  const int dims[4] = {2 * lane, 2 * lane + 1, 64 + 2 * lane, 64 + 2 * lane + 1};
+  if (!train) return;
+  if (k == 0 || t < 0) { /* no target: this row adds no gradient */
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      dQ[(size_t)i * kOut + dims[u]] = __float2bfloat16(0.f);
+      dQt[(size_t)dims[u] * rows + i] = __float2bfloat16(0.f);
+    }
+    return;
+  }
+  /* softmax denominator */
+  float z = 0.f;
+  for (int j = lane; j < k; j += 32) z += __expf(mylog[j >> 5] - mx);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) z += __shfl_xor_sync(0xFFFFFFFFu, z, o);
+  const float lt = __shfl_sync(0xFFFFFFFFu, mylog[t >> 5], t & 31);
+  if (lane == 0) {
+    atomicAdd(loss, (mx + logf(z)) - lt);
+    if (arg == t) atomicAdd(correct, 1u);
+  }
+  /* pass 2: gradients */
+  float gf0 = 0.f, gf1 = 0.f, gt0 = 0.f, gt1 = 0.f;
+  for (int j = 0; j < k; j++) {
+    const float x = __shfl_sync(0xFFFFFFFFu, mylog[j >> 5], j & 31);
+    const float dl = (__expf(x - mx) / z - (j == t ? 1.f : 0.f)) * inv_count;
+    const uint16_t mv = moves[(size_t)i * kMaxLegal + j];
+    const int f = mv & 63, to = mv >> 6;
+    gf0 += dl * Ef[f * 64 + 2 * lane];
+    gf1 += dl * Ef[f * 64 + 2 * lane + 1];
+    gt0 += dl * Et[to * 64 + 2 * lane];
+    gt1 += dl * Et[to * 64 + 2 * lane + 1];
+    atomicAdd(&grads[OFF_EF + f * 64 + 2 * lane], dl * qf0);
+    atomicAdd(&grads[OFF_EF + f * 64 + 2 * lane + 1], dl * qf1);
+    atomicAdd(&grads[OFF_ET + to * 64 + 2 * lane], dl * qt0);
+    atomicAdd(&grads[OFF_ET + to * 64 + 2 * lane + 1], dl * qt1);
+  }
+  const float g[4] = {gf0, gf1, gt0, gt1};
+#pragma unroll
+  for (int u = 0; u < 4; u++) {
+    dQ[(size_t)i * kOut + dims[u]] = __float2bfloat16(g[u]);
+    dQt[(size_t)dims[u] * rows + i] = __float2bfloat16(g[u]);
+  }
+}
+
+/* column sums of a rows x cols bf16 matrix into out (bias gradients) */
+__global__ void k_colsum(const bf16 *__restrict__ Y, int rows, int cols, float *out) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= cols) return;
+  float s = 0.f;
+  for (int r = 0; r < rows; r++) s += __bfloat162float(Y[(size_t)r * cols + c]);
+  out[c] = s;
+}
+
+/* Adam on the flat parameter vector */
+__global__ void k_adam(float *p, const float *g, float *m, float *v, size_t n, float lr, float b1, float b2,
+                       float eps, float c1, float c2) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float gi = g[i];
+  float mi = b1 * m[i] + (1.f - b1) * gi, vi = b2 * v[i] + (1.f - b2) * gi * gi;
+  m[i] = mi;
+  v[i] = vi;
+  p[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+}
+
+/* BF16 copies of a rows x cols FP32 weight: as is, and transposed */
+__global__ void k_to_bf16(const float *__restrict__ W, int rows, int cols, bf16 *Wb, bf16 *Wt) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (size_t)rows * cols) return;
+  int r = (int)(i / cols), c = (int)(i % cols);
+  bf16 x = __float2bfloat16(W[i]);
+  if (Wb) Wb[i] = x;
+  if (Wt) Wt[(size_t)c * rows + r] = x;
+}
+
+/* FP8 E4M3 copy with a per-tensor scale: q = x / scale, scale = max|x|/448 */
+__global__ void k_absmax(const float *__restrict__ x, size_t n, unsigned *out_bits) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  float a = i < n ? fabsf(x[i]) : 0.f;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) a = fmaxf(a, __shfl_xor_sync(0xFFFFFFFFu, a, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(out_bits, __float_as_uint(a)); /* non-negative floats order as ints */
+}
+__global__ void k_absmax_bf16(const bf16 *__restrict__ x, size_t n, unsigned *out_bits) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  float a = i < n ? fabsf(__bfloat162float(x[i])) : 0.f;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) a = fmaxf(a, __shfl_xor_sync(0xFFFFFFFFu, a, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(out_bits, __float_as_uint(a));
+}
+__global__ void k_quant_fp8(const float *__restrict__ xf, const bf16 *__restrict__ xb, size_t n,
+                            const unsigned *absmax_bits, __nv_fp8_e4m3 *q) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float am = __uint_as_float(*absmax_bits);
+  float inv = am > 0.f ? 448.f / am : 1.f;
+  float x = xf ? xf[i] : __bfloat162float(xb[i]);
+  q[i] = __nv_fp8_e4m3(x * inv);
+}
+
+/* ---------------- state ---------------- */
+struct MlpState {
+  float *params = nullptr, *grads = nullptr, *m = nullptr, *v = nullptr;
+  bf16 *W1b = nullptr, *W2b = nullptr, *W3b = nullptr, *W2t = nullptr, *W3t = nullptr;
+  __nv_fp8_e4m3 *W1q = nullptr, *W2q = nullptr, *W3q = nullptr;
+  unsigned *amax = nullptr; /* [0..2] weights, [3..5] activations (float bits) */
+  int cap = 0;              /* activation rows */
+  bf16 *X = nullptr, *Xt = nullptr, *H1 = nullptr, *H1t = nullptr, *H2 = nullptr, *H2t = nullptr;
+  bf16 *dQ = nullptr, *dQt = nullptr, *dH2 = nullptr, *dH2t = nullptr, *dH1 = nullptr, *dH1t = nullptr;
+  __nv_fp8_e4m3 *Xq = nullptr, *H1q = nullptr, *H2q = nullptr;
+  float *Q = nullptr, *scores = nullptr;
+  uint16_t *moves = nullptr;
+  uint8_t *nmoves = nullptr;
+  int16_t *tidx = nullptr;
+  float *loss = nullptr;
+  unsigned *correct = nullptr;
+  uint32_t *err = nullptr;
+  uint64_t *d_boards = nullptr;
+  uint8_t *d_stm = nullptr;
+  Move *d_targets = nullptr;
+  int data_cap = 0;
+  int step = 0;
+};
+
+MlpState *state() { return (MlpState *)ctx().mlp; }
+
+unsigned long long g_rng;
+float urand() { /* splitmix64 -> [0,1) */
+  unsigned long long z = (g_rng += 0x9E3779B97F4A7C15ULL);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+  z ^= z >> 31;
+  return (float)((z >> 11) * (1.0 / 9007199254740992.0));
+}
+
+template <typename T>
+int dalloc(T *&p, size_t n) {
+  ZCHECK(cudaMalloc(&p, n * sizeof(T)));
+  return ZETA_OK;
+}
+
+int ensure_rows(MlpState &S, int rows) {
+  if (rows <= S.cap) return ZETA_OK;
+  void *bufs[] = {S.X, S.Xt, S.H1, S.H1t, S.H2, S.H2t, S.dQ, S.dQt, S.dH2, S.dH2t, S.dH1, S.dH1t,
+                  S.Xq, S.H1q, S.H2q, S.Q, S.scores, S.moves, S.nmoves, S.tidx};
+  for (void *b : bufs) cudaFree(b);
+  const size_t R = (size_t)rows;
+  int rc = 0;
+  rc |= dalloc(S.X, R * kIn) | dalloc(S.Xt, R * kIn) | dalloc(S.H1, R * kH1) | dalloc(S.H1t, R * kH1);
+  rc |= dalloc(S.H2, R * kH2) | dalloc(S.H2t, R * kH2) | dalloc(S.dQ, R * kOut) | dalloc(S.dQt, R * kOut);
+  rc |= dalloc(S.dH2, R * kH2) | dalloc(S.dH2t, R * kH2) | dalloc(S.dH1, R * kH1) | dalloc(S.dH1t, R * kH1);
+  rc |= dalloc(S.Xq, R * kIn) | dalloc(S.H1q, R * kH1) | dalloc(S.H2q, R * kH2) | dalloc(S.Q, R * kOut);
+  rc |= dalloc(S.scores, R * kMaxLegal) | dalloc(S.moves, R * kMaxLegal) | dalloc(S.nmoves, R) | dalloc(S.tidx, R);
+  if (rc) return ZETA_ERR_CUDA;
+  S.cap = rows;
+  return ZETA_OK;
+}
+
+/* BF16 and FP8 copies of the weights after every update */
+int refresh_weights(MlpState &S, cudaStream_t s) {
+  auto grid = [](size_t n) { return (unsigned)((n + 255) / 256); };
+  k_to_bf16<<<grid((size_t)kH1 * kIn), 256, 0, s>>>(S.params + OFF_W1, kH1, kIn, S.W1b, nullptr);
+  k_to_bf16<<<grid((size_t)kH2 * kH1), 256, 0, s>>>(S.params + OFF_W2, kH2, kH1, S.W2b, S.W2t);
+  k_to_bf16<<<grid((size_t)kOut * kH2), 256, 0, s>>>(S.params + OFF_W3, kOut, kH2, S.W3b, S.W3t);
+  ZCHECK(cudaMemsetAsync(S.amax, 0, 3 * sizeof(unsigned), s));
+  const size_t off[3] = {OFF_W1, OFF_W2, OFF_W3}, num[3] = {(size_t)kH1 * kIn, (size_t)kH2 * kH1, (size_t)kOut * kH2};
+  __nv_fp8_e4m3 *q[3] = {S.W1q, S.W2q, S.W3q};
+  for (int i = 0; i < 3; i++) {
+    k_absmax<<<grid(num[i]), 256, 0, s>>>(S.params + off[i], num[i], S.amax + i);
+    k_quant_fp8<<<grid(num[i]), 256, 0, s>>>(S.params + off[i], nullptr, num[i], S.amax + i, q[i]);
+  }
+  ZCHECK(cudaGetLastError());
+  return ZETA_OK;
+}
+
+int mlp_create(unsigned long long seed) {
+  Context &c = ctx();
+  if (!c.mlp) c.mlp = new MlpState();
+  MlpState &S = *state();
+  if (!S.params) {
+    int rc = dalloc(S.params, NPARAM) | dalloc(S.grads, NPARAM) | dalloc(S.m, NPARAM) | dalloc(S.v, NPARAM);
+    rc |= dalloc(S.W1b, (size_t)kH1 * kIn) | dalloc(S.W2b, (size_t)kH2 * kH1) | dalloc(S.W3b, (size_t)kOut * kH2);
+    rc |= dalloc(S.W2t, (size_t)kH2 * kH1) | dalloc(S.W3t, (size_t)kOut * kH2);
+    rc |= dalloc(S.W1q, (size_t)kH1 * kIn) | dalloc(S.W2q, (size_t)kH2 * kH1) | dalloc(S.W3q, (size_t)kOut * kH2);
+    rc |= dalloc(S.amax, 8) | dalloc(S.loss, 1) | dalloc(S.correct, 1) | dalloc(S.err, 1);
+    if (rc) return ZETA_ERR_CUDA;
+  }
+  /* He-uniform weights, zero biases, small embeddings */
+  std::vector<float> h(NPARAM, 0.f);
+  g_rng = seed;
+  auto fill = [&](size_t off, size_t n, float lim) {
+    for (size_t i = 0; i < n; i++) h[off + i] = (2.f * urand() - 1.f) * lim;
+  };
+  fill(OFF_W1, (size_t)kH1 * kIn, sqrtf(6.f / 32.f)); /* about 32 active inputs */
+  fill(OFF_W2, (size_t)kH2 * kH1, sqrtf(6.f / kH1));
+  fill(OFF_W3, (size_t)kOut * kH2, sqrtf(3.f / kH2));
+  fill(OFF_EF, (size_t)64 * kEmb, 0.5f);
+  fill(OFF_ET, (size_t)64 * kEmb, 0.5f);
+  ZCHECK(cudaMemcpy(S.params, h.data(), NPARAM * sizeof(float), cudaMemcpyHostToDevice));
+  ZCHECK(cudaMemset(S.m, 0, NPARAM * sizeof(float)));
+  ZCHECK(cudaMemset(S.v, 0, NPARAM * sizeof(float)));
+  S.step = 0;
+  int rc = refresh_weights(S, c.stream);
+  if (rc) return rc;
+  ZCHECK(cudaStreamSynchronize(c.stream));
+  return ZETA_OK;
+}
+
+GemmArgs gemm(const void *A, const void *B, int M, int N, int K, uint32_t *err) {
+  GemmArgs g{A, B, M, N, K, nullptr, 0, nullptr, nullptr, nullptr, 1.f, err, nullptr, nullptr, nullptr};
+  return g;
+}
+
+/* features, move lists and the forward pass of `rows` positions
+ * (rows a multiple of 128; n real ones) */
+int forward(MlpState &S, const uint64_t *d_boards, const uint8_t *d_stm, const Move *d_targets, int n, int rows,
+            bool fp8, cudaStream_t s) {
+  int rc;
+  ZCHECK(cudaMemsetAsync(S.X, 0, (size_t)rows * kIn * sizeof(bf16), s));
+  ZCHECK(cudaMemsetAsync(S.Xt, 0, (size_t)rows * kIn * sizeof(bf16), s));
+  k_features<<<(rows + 127) / 128, 128, 0, s>>>(d_boards, d_stm, d_targets, n, rows, S.X, S.Xt, S.moves, S.nmoves,
+                                                S.tidx);
+  ZCHECK(cudaGetLastError());
+  const float *P = S.params;
+  if (!fp8) {
+    GemmArgs g1 = gemm(S.X, S.W1b, rows, kH1, kIn, S.err);
+    g1.bias = P + OFF_B1, g1.relu = 1, g1.Cb = S.H1, g1.Ct = S.H1t;
+    if ((rc = gemm_launch(g1, false, s))) return rc;
+    GemmArgs g2 = gemm(S.H1, S.W2b, rows, kH2, kH1, S.err);
+    g2.bias = P + OFF_B2, g2.relu = 1, g2.Cb = S.H2, g2.Ct = S.H2t;
+    if ((rc = gemm_launch(g2, false, s))) return rc;
+    GemmArgs g3 = gemm(S.H2, S.W3b, rows, kOut, kH2, S.err);
+    g3.bias = P + OFF_B3, g3.Cf = S.Q;
+    return gemm_launch(g3, false, s);
+  }
+  /* FP8 E4M3 inference: per-tensor scales of the activations, measured */
+  auto grid = [](size_t n) { return (unsigned)((n + 255) / 256); };
+  ZCHECK(cudaMemsetAsync(S.amax + 3, 0, 3 * sizeof(unsigned), s));
+  size_t nx = (size_t)rows * kIn;
+  k_absmax_bf16<<<grid(nx), 256, 0, s>>>(S.X, nx, S.amax + 3);
+  k_quant_fp8<<<grid(nx), 256, 0, s>>>(nullptr, S.X, nx, S.amax + 3, S.Xq);
+  GemmArgs g1 = gemm(S.Xq, S.W1q, rows, kH1, kIn, S.err);
+  g1.bias = P + OFF_B1, g1.relu = 1, g1.Cb = S.H1, g1.amaxA = S.amax + 3, g1.amaxB = S.amax + 0;
+  if ((rc = gemm_launch(g1, true, s))) return rc;
+  size_t nh1 = (size_t)rows * kH1;
+  k_absmax_bf16<<<grid(nh1), 256, 0, s>>>(S.H1, nh1, S.amax + 4);
+  k_quant_fp8<<<grid(nh1), 256, 0, s>>>(nullptr, S.H1, nh1, S.amax + 4, S.H1q);
+  GemmArgs g2 = gemm(S.H1q, S.W2q, rows, kH2, kH1, S.err);
+  g2.bias = P + OFF_B2, g2.relu = 1, g2.Cb = S.H2, g2.amaxA = S.amax + 4, g2.amaxB = S.amax + 1;
+  if ((rc = gemm_launch(g2, true, s))) return rc;
+  size_t nh2 = (size_t)rows * kH2;
+  k_absmax_bf16<<<grid(nh2), 256, 0, s>>>(S.H2, nh2, S.amax + 5);
+  k_quant_fp8<<<grid(nh2), 256, 0, s>>>(nullptr, S.H2, nh2, S.amax + 5, S.H2q);
+  GemmArgs g3 = gemm(S.H2q, S.W3q, rows, kOut, kH2, S.err);
+  g3.bias = P + OFF_B3, g3.Cf = S.Q, g3.amaxA = S.amax + 5, g3.amaxB = S.amax + 2;
+  return gemm_launch(g3, true, s);
+}
+
+/* loss head and the backward pass into S.grads (mean over n positions) */
+int backward(MlpState &S, int n, int rows, cudaStream_t s) {
+  int rc;
+  ZCHECK(cudaMemsetAsync(S.grads, 0, NPARAM * sizeof(float), s));
+  k_head<<<(rows * 32 + 127) / 128, 128, 0, s>>>(S.Q, S.params, S.moves, S.nmoves, S.tidx, rows, 1.f / (float)n, 1,
+                                                 S.dQ, S.dQt, S.grads, S.loss, S.correct, nullptr);
+  ZCHECK(cudaGetLastError());
+  float *G = S.grads;
+  GemmArgs a = gemm(S.dQ, S.W3t, rows, kH2, kOut, S.err); /* dH2 = dQ W3 . relu'(H2) */
+  a.mask = S.H2, a.Cb = S.dH2, a.Ct = S.dH2t;
+  if ((rc = gemm_launch(a, false, s))) return rc;
+  GemmArgs b = gemm(S.dQt, S.H2t, kOut, kH2, rows, S.err); /* dW3 = dQ^T H2 */
+  b.Cf = G + OFF_W3;
+  if ((rc = gemm_launch(b, false, s))) return rc;
+  GemmArgs c = gemm(S.dH2, S.W2t, rows, kH1, kH2, S.err); /* dH1 = dH2 W2 . relu'(H1) */
+  c.mask = S.H1, c.Cb = S.dH1, c.Ct = S.dH1t;
+  if ((rc = gemm_launch(c, false, s))) return rc;
+  GemmArgs d = gemm(S.dH2t, S.H1t, kH2, kH1, rows, S.err); /* dW2 = dH2^T H1 */
+  d.Cf = G + OFF_W2;
+  if ((rc = gemm_launch(d, false, s))) return rc;
+  GemmArgs e = gemm(S.dH1t, S.Xt, kH1, kIn, rows, S.err); /* dW1 = dH1^T X */
+  e.Cf = G + OFF_W1;
+  if ((rc = gemm_launch(e, false, s))) return rc;
+  k_colsum<<<(kOut + 127) / 128, 128, 0, s>>>(S.dQ, rows, kOut, G + OFF_B3);
+  k_colsum<<<(kH2 + 127) / 128, 128, 0, s>>>(S.dH2, rows, kH2, G + OFF_B2);
+  k_colsum<<<(kH1 + 127) / 128, 128, 0, s>>>(S.dH1, rows, kH1, G + OFF_B1);
+  ZCHECK(cudaGetLastError());
+  return ZETA_OK;
+}
+
+int load_data(MlpState &S, const uint64_t *boards, const uint8_t *stm, const uint32_t *targets, int n,
+              cudaStream_t s) {
+  if (n > S.data_cap) {
+    cudaFree(S.d_boards);
+    cudaFree(S.d_stm);
+    cudaFree(S.d_targets);
+    S.data_cap = 0;
+    int rc = dalloc(S.d_boards, (size_t)n * 7) | dalloc(S.d_stm, (size_t)n) | dalloc(S.d_targets, (size_t)n);
+    if (rc) return ZETA_ERR_CUDA;
+    S.data_cap = n;
+  }
+  ZCHECK(cudaMemcpyAsync(S.d_boards, boards, (size_t)n * 56, cudaMemcpyHostToDevice, s));
+  ZCHECK(cudaMemcpyAsync(S.d_stm, stm, (size_t)n, cudaMemcpyHostToDevice, s));
+  if (targets) ZCHECK(cudaMemcpyAsync(S.d_targets, targets, (size_t)n * 4, cudaMemcpyHostToDevice, s));
+  return ZETA_OK;
+}
+
+int check_err(MlpState &S, cudaStream_t s) {
+  uint32_t e = 0;
+  ZCHECK(cudaMemcpyAsync(&e, S.err, 4, cudaMemcpyDeviceToHost, s));
+  ZCHECK(cudaStreamSynchronize(s));
+  if (e) return set_error(ZETA_ERR_BUDGET, "mlp: a tensor-core wait timed out");
+  return ZETA_OK;
+}
+
+}  // namespace
+
+void mlp_free() {
+  Context &c = ctx();
+  MlpState *S = (MlpState *)c.mlp;
+  if (!S) return;
+  void *bufs[] = {S->params, S->grads, S->m, S->v, S->W1b, S->W2b, S->W3b, S->W2t, S->W3t, S->W1q, S->W2q,
+                  S->W3q, S->amax, S->X, S->Xt, S->H1, S->H1t, S->H2, S->H2t, S->dQ, S->dQt, S->dH2, S->dH2t,
+                  S->dH1, S->dH1t, S->Xq, S->H1q, S->H2q, S->Q, S->scores, S->moves, S->nmoves, S->tidx,
+                  S->loss, S->correct, S->err, S->d_boards, S->d_stm, S->d_targets};
+  for (void *b : bufs) cudaFree(b);
+  delete S;
+  c.mlp = nullptr;
+}
+
+}  // namespace zeta
+
+static int mlp_ready() {
+  if (!zeta::ctx().ready) return set_error(ZETA_ERR_STATE, "zeta_init has not been called");
+  if (!zeta::ctx().mlp || !((zeta::MlpState *)zeta::ctx().mlp)->params)
+    return set_error(ZETA_ERR_STATE, "zeta_mlp_init has not been called");
+  return ZETA_OK;
+}
+
+extern "C" {
+
+int zeta_mlp_init(uint64_t seed) {
+  if (!ctx().ready) return set_error(ZETA_ERR_STATE, "zeta_init has not been called");
+  return mlp_create(seed);
+}
+
+int zeta_mlp_param_count(void) { return (int)NPARAM; }
+
+int zeta_mlp_get_params(float *out) {
+  int rc = mlp_ready();
+  if (rc) return rc;
+  ZCHECK(cudaMemcpy(out, state()->params, NPARAM * sizeof(float), cudaMemcpyDeviceToHost));
+  return ZETA_OK;
+}
+
+int zeta_mlp_set_params(const float *in) {
+  int rc = mlp_ready();
+  if (rc) return rc;
+  MlpState &S = *state();
+  ZCHECK(cudaMemcpy(S.params, in, NPARAM * sizeof(float), cudaMemcpyHostToDevice));
+  rc = refresh_weights(S, ctx().stream);
+  if (rc) return rc;
+  ZCHECK(cudaStreamSynchronize(ctx().stream));
+  return ZETA_OK;
+}
+
+/* One batch: forward, loss and gradients (no update).  grads: NPARAM
+ * floats in the flat layout of zeta_mlp_get_params; loss: mean. */
+int zeta_mlp_grads(const uint64_t *boards, const uint8_t *stm, const uint32_t *targets, int n, float *grads,
+                   float *loss) {
+  int rc = mlp_ready();
+  if (rc) return rc;
+  if (n <= 0) return set_error(ZETA_ERR_ARG, "empty batch");
+  MlpState &S = *state();
+  cudaStream_t s = ctx().stream;
+  const int rows = (n + 127) / 128 * 128;
+  if ((rc = ensure_rows(S, rows)) || (rc = load_data(S, boards, stm, targets, n, s))) return rc;
+  ZCHECK(cudaMemsetAsync(S.err, 0, 4, s));
+  ZCHECK(cudaMemsetAsync(S.loss, 0, 4, s));
+  ZCHECK(cudaMemsetAsync(S.correct, 0, 4, s));
+  if ((rc = forward(S, S.d_boards, S.d_stm, S.d_targets, n, rows, false, s))) return rc;
+  if ((rc = backward(S, n, rows, s))) return rc;
+  if ((rc = check_err(S, s))) return rc;
+  if (grads) ZCHECK(cudaMemcpy(grads, S.grads, NPARAM * sizeof(float), cudaMemcpyDeviceToHost));
+  float l = 0;
+  ZCHECK(cudaMemcpy(&l, S.loss, 4, cudaMemcpyDeviceToHost));
+  if (loss) *loss = l / (float)n;
+  return ZETA_OK;
+}
+
+/* Adam training over (boards, stm, best move) examples, `epochs` passes in
+ * order, batches of `batch` (a multiple of 128).  Per epoch: mean loss
+ * and the share of examples whose highest-scored legal move is the
+ * target (the model's state before each update). */
+int zeta_mlp_train(const uint64_t *boards, const uint8_t *stm, const uint32_t *targets, int n, int epochs, int batch,
+                   float lr, float *loss_per_epoch, float *acc_per_epoch) {
+  int rc = mlp_ready();
+  if (rc) return rc;
+  if (n <= 0 || epochs <= 0 || batch <= 0 || batch % 128) return set_error(ZETA_ERR_ARG, "bad training arguments");
+  MlpState &S = *state();
+  cudaStream_t s = ctx().stream;
+  if ((rc = ensure_rows(S, batch)) || (rc = load_data(S, boards, stm, targets, n, s))) return rc;
+  ZCHECK(cudaMemsetAsync(S.err, 0, 4, s));
+  const float b1 = 0.9f, b2 = 0.999f;
+  for (int ep = 0; ep < epochs; ep++) {
+    ZCHECK(cudaMemsetAsync(S.loss, 0, 4, s));
+    ZCHECK(cudaMemsetAsync(S.correct, 0, 4, s));
+    for (int off = 0; off < n; off += batch) {
+      const int cnt = n - off < batch ? n - off : batch;
+      const int rows = (cnt + 127) / 128 * 128;
+      if ((rc = forward(S, S.d_boards + 7 * (size_t)off, S.d_stm + off, S.d_targets + off, cnt, rows, false, s)))
+        return rc;
+      if ((rc = backward(S, cnt, rows, s))) return rc;
+      S.step++;
+      const float c1 = 1.f - powf(b1, (float)S.step), c2 = 1.f - powf(b2, (float)S.step);
+      k_adam<<<(unsigned)((NPARAM + 255) / 256), 256, 0, s>>>(S.params, S.grads, S.m, S.v, NPARAM, lr, b1, b2, 1e-8f,
+                                                             c1, c2);
+      ZCHECK(cudaGetLastError());
+      if ((rc = refresh_weights(S, s))) return rc;
+    }
+    float l = 0;
+    unsigned corr = 0;
+    ZCHECK(cudaMemcpyAsync(&l, S.loss, 4, cudaMemcpyDeviceToHost, s));
+    ZCHECK(cudaMemcpyAsync(&corr, S.correct, 4, cudaMemcpyDeviceToHost, s));
+    if ((rc = check_err(S, s))) return rc;
+    if (loss_per_epoch) loss_per_epoch[ep] = l / (float)n;
+    if (acc_per_epoch) acc_per_epoch[ep] = (float)corr / (float)n;
+  }
+  return ZETA_OK;
+}
+
+/* Scores of every legal move of n positions (BF16, or FP8 E4M3 when fp8 !=
+ * 0): scores n x 218 floats in the order of the engine's move generator,
+ * nmoves n counts; the engine orders by them.  best (optional): index of
+ * the highest score. */
+int zeta_mlp_scores(const uint64_t *boards, const uint8_t *stm, int n, int fp8, float *scores, uint8_t *nmoves,
+                    int32_t *best) {
+  int rc = mlp_ready();
+  if (rc) return rc;
+  if (n <= 0) return set_error(ZETA_ERR_ARG, "empty batch");
+  MlpState &S = *state();
+  cudaStream_t s = ctx().stream;
+  const int rows = (n + 127) / 128 * 128;
+  if ((rc = ensure_rows(S, rows)) || (rc = load_data(S, boards, stm, nullptr, n, s))) return rc;
+  ZCHECK(cudaMemsetAsync(S.err, 0, 4, s));
+  if ((rc = forward(S, S.d_boards, S.d_stm, nullptr, n, rows, fp8 != 0, s))) return rc;
+  k_head<<<(rows * 32 + 127) / 128, 128, 0, s>>>(S.Q, S.params, S.moves, S.nmoves, S.tidx, rows, 1.f, 0, nullptr,
+                                                 nullptr, nullptr, nullptr, nullptr, S.scores);
+  ZCHECK(cudaGetLastError());
+  if ((rc = check_err(S, s))) return rc;
+  std::vector<float> sc((size_t)n * kMaxLegal);
+  std::vector<uint8_t> nm(n);
+  ZCHECK(cudaMemcpy(sc.data(), S.scores, sc.size() * 4, cudaMemcpyDeviceToHost));
+  ZCHECK(cudaMemcpy(nm.data(), S.nmoves, n, cudaMemcpyDeviceToHost));
+  if (scores) memcpy(scores, sc.data(), sc.size() * 4);
+  if (nmoves) memcpy(nmoves, nm.data(), n);
+  if (best)
+    for (int i = 0; i < n; i++) {
+      int b = -1;
+      float bv = -1e30f;
+      for (int j = 0; j < nm[i]; j++)
+        if (sc[(size_t)i * kMaxLegal + j] > bv) bv = sc[(size_t)i * kMaxLegal + j], b = j;
+      best[i] = b;
+    }
+  return ZETA_OK;
+}
+
+}  // extern "C"

@@ -228,14 +228,15 @@ template <int TPB>
 __global__ void __launch_bounds__(TPB) k_search_pure(const uint64_t *__restrict__ boards, const uint8_t *__restrict__ stm,
                                                      int N, int nworkers, int depth, TTEntry *tt, u64 tt_mask,
                                                      uint32_t *busy, u64 busy_mask, uint32_t *done, SearchOut *out,
-                                                     unsigned long long budget, uint32_t *status) {
+                                                     unsigned long long budget, uint32_t *status, uint32_t *active,
+                                                     int max_per_pos) {
   __shared__ EvalTables sT;
   for (int i = threadIdx.x; i < (int)(sizeof(EvalTables) / 4); i += TPB)
     ((uint32_t *)&sT)[i] = ((const uint32_t *)&kEvalDev)[i];
   __syncthreads();
   const long long t = (long long)blockIdx.x * TPB + threadIdx.x;
   if (t >= (long long)N * nworkers) return;
-  const int p = (int)(t % N);
+  int p = (int)(t % N);
 
   Frame F[kMaxSearchDepth + 1];
   Worker W;
@@ -244,36 +245,59 @@ __global__ void __launch_bounds__(TPB) k_search_pure(const uint64_t *__restrict_
   W.busy = busy;
   W.busy_mask = busy_mask;
   W.T = &sT;
-  W.nodes = W.tthits = 0;
-  for (int i = 0; i <= kMaxSearchDepth; i++) W.killer[i][0] = W.killer[i][1] = 0;
-
-  const uint64_t *b = boards + 7 * (size_t)p;
-  F[0].pos.b0 = b[0];
-  F[0].pos.p1 = b[1];
-  F[0].pos.p2 = b[2];
-  F[0].pos.p3 = b[3];
-  F[0].pos.cr = b[4];
-  F[0].stm = stm[p] & 1;
-  F[0].depth = depth;
-  F[0].alpha = -kSearchInf - 1;
-  F[0].beta = kSearchInf + 1;
-  F[0].exclusive = 0;
-  int v;
-  if (!node_enter(W, F[0], 0, v)) {
-    /* no legal move at the root: the game is over */
-    if (atomicCAS(&done[p], 0u, 1u) == 0u) {
-      out[p].score = v;
-      out[p].bestmove = 0;
-    }
-    atomicAdd(&out[p].nodes, W.nodes);
-    return;
-  }
-  int ply = 0;
   unsigned long long steps = 0;
-  for (;;) {
+
+  /* A worker searches its own position, then helps unfinished ones: it
+   * joins them as one more ABDADA worker from their root, so the largest
+   * trees of the batch end up with every thread of the grid. */
+  for (int job = 0;; job++) {
+    if (job > 0) {
+      if (max_per_pos <= nworkers) break; /* helping disabled */
+      const unsigned h = (unsigned)(t * 0x9E3779B1u + (unsigned)job * 0x85EBCA6Bu);
+      int q = -1;
+      for (int k = 0; k < N; k++) {
+        int c = (int)((h + (unsigned)k) % (unsigned)N);
+        if (((volatile uint32_t *)done)[c]) continue;
+        if (atomicAdd(&active[c], 1u) < (unsigned)max_per_pos) {
+          q = c;
+          break;
+        }
+        atomicSub(&active[c], 1u);
+      }
+      if (q < 0) break;
+      p = q;
+    } else {
+      atomicAdd(&active[p], 1u);
+    }
+    W.nodes = W.tthits = 0;
+    for (int i = 0; i <= kMaxSearchDepth; i++) W.killer[i][0] = W.killer[i][1] = 0;
+    const uint64_t *b = boards + 7 * (size_t)p;
+    F[0].pos.b0 = b[0];
+    F[0].pos.p1 = b[1];
+    F[0].pos.p2 = b[2];
+    F[0].pos.p3 = b[3];
+    F[0].pos.cr = b[4];
+    F[0].stm = stm[p] & 1;
+    F[0].depth = depth;
+    F[0].alpha = -kSearchInf - 1;
+    F[0].beta = kSearchInf + 1;
+    F[0].exclusive = 0;
+    int v;
+    if (!node_enter(W, F[0], 0, v)) {
+      /* no legal move at the root: the game is over */
+      if (atomicCAS(&done[p], 0u, 1u) == 0u) {
+        out[p].score = v;
+        out[p].bestmove = 0;
+      }
+      atomicAdd(&out[p].nodes, W.nodes);
+      atomicSub(&active[p], 1u);
+      continue;
+    }
+    int ply = 0;
+    for (;;) {
     if (++steps > budget) {
       atomicOr(status, SST_BUDGET);
-      break;
+      return;
     }
     if ((steps & 15) == 0 && ((volatile uint32_t *)done)[p]) break; /* another worker finished */
     Frame &f = F[ply];
@@ -348,9 +372,11 @@ __global__ void __launch_bounds__(TPB) k_search_pure(const uint64_t *__restrict_
       h.i = h.n; /* cut: nothing else to search here */
       h.deferred = 0;
     }
+    }
+    atomicAdd(&out[p].nodes, W.nodes);
+    atomicAdd(&out[p].tthits, W.tthits);
+    atomicSub(&active[p], 1u);
   }
-  atomicAdd(&out[p].nodes, W.nodes);
-  atomicAdd(&out[p].tthits, W.tthits);
 }
 
 __global__ void k_search_scatter(const SearchOut *out, int n, int32_t *scores, uint32_t *moves,
@@ -375,7 +401,8 @@ static int search_buffers(int n) {
     c.s_done = nullptr;
     c.s_cap = 0;
     ZCHECK(cudaMalloc(&c.s_out, (size_t)n * sizeof(SearchOut)));
-    ZCHECK(cudaMalloc(&c.s_done, (size_t)n * sizeof(uint32_t)));
+    /* done flags, then active-worker counts */
+    ZCHECK(cudaMalloc(&c.s_done, (size_t)2 * n * sizeof(uint32_t)));
     c.s_cap = n;
   }
   if (!c.s_busy) {
@@ -409,7 +436,7 @@ int search_pure_launch(const uint64_t *d_boards, const uint8_t *d_stm, int n, in
   TTEntry *tt = (TTEntry *)(c.tt1 ? c.tt1 : c.s_tt);
   u64 entries = c.tt1 ? c.tt1_entries : c.s_tt_entries;
   ZCHECK(cudaMemsetAsync(c.s_out, 0, (size_t)n * sizeof(SearchOut), s));
-  ZCHECK(cudaMemsetAsync(c.s_done, 0, (size_t)n * sizeof(uint32_t), s));
+  ZCHECK(cudaMemsetAsync(c.s_done, 0, (size_t)2 * n * sizeof(uint32_t), s));
   ZCHECK(cudaMemsetAsync(c.s_busy, 0, c.s_busy_entries * sizeof(uint32_t), s));
   ZCHECK(cudaMemsetAsync(c.s_status, 0, sizeof(uint32_t), s));
   const long long threads = (long long)n * workers;
@@ -418,7 +445,7 @@ int search_pure_launch(const uint64_t *d_boards, const uint8_t *d_stm, int n, in
   ZCHECK(cudaEventRecord(c.ev[1], s));
   k_search_pure<128><<<(unsigned)((threads + tpb - 1) / tpb), tpb, 0, s>>>(
       d_boards, d_stm, n, workers, depth, tt, entries - 1, c.s_busy, c.s_busy_entries - 1, c.s_done,
-      (SearchOut *)c.s_out, budget, c.s_status);
+      (SearchOut *)c.s_out, budget, c.s_status, c.s_done + n, c.s_helpers_cap);
   ZCHECK(cudaGetLastError());
   ZCHECK(cudaEventRecord(c.ev[2], s));
   k_search_scatter<<<(n + 127) / 128, 128, 0, s>>>((const SearchOut *)c.s_out, n, d_scores, d_moves, d_nodes);

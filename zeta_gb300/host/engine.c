@@ -1,0 +1,168 @@
+/*
+ * engine.c -- host drivers of the device path: perft (src/search.c:225-271),
+ * selftest (src/test.c:36-169) and iterative-deepening rootsearch
+ * (src/search.c:35-223), all through the clrun.h calls.
+ */
+#include <inttypes.h>
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#include <time.h>
+
+#include "../../include/clrun.h"
+#include "engine.h"
+
+Bitboard BOARD[7];
+int STM = WHITE, SD = MAXPLY - 1, PLY = 0, GAMEPLY = 0;
+Bitboard HashHistory[MAXGAMEPLY];
+Move MoveHistory[MAXGAMEPLY];
+Bitboard GLOBAL_BOARD[7];
+uint64_t *COUNTERS = NULL;
+uint32_t *PV = NULL;
+uint64_t *GLOBAL_HASHHISTORY = NULL;
+uint32_t *RNUMBERS = NULL;
+uint64_t threadsX = 1, threadsY = 1, totalWorkUnits = 1;
+uint64_t tt1_memory = 256, tt2_memory = 0;
+int64_t nodes_per_second = 1000000;
+uint64_t MaxNodes = 0;
+int device_id = 0;
+int search_mode = 0;
+uint64_t ABNODECOUNT = 0, TTHITS = 0, TTSCOREHITS = 0, IIDHITS = 0;
+FILE *LogFile = NULL;
+
+double get_time_ms(void) {
+  struct timespec t;
+  clock_gettime(CLOCK_MONOTONIC, &t);
+  return t.tv_sec * 1000.0 + t.tv_nsec / 1e6;
+}
+
+/* read_and_init_config, src/io.c:533-583: the same keys; a missing file
+ * keeps the defaults (one worker, 256 MB table) */
+bool read_config(const char *path) {
+  FILE *f = fopen(path, "r");
+  if (!f) return false;
+  char line[1024];
+  while (fgets(line, sizeof line, f)) {
+    sscanf(line, "threadsX: %" SCNu64 ";", &threadsX);
+    sscanf(line, "threadsY: %" SCNu64 ";", &threadsY);
+    sscanf(line, "nodes_per_second: %" SCNi64 ";", &nodes_per_second);
+    sscanf(line, "tt1_memory: %" SCNu64 ";", &tt1_memory);
+    sscanf(line, "tt2_memory: %" SCNu64 ";", &tt2_memory);
+    sscanf(line, "device_id: %d;", &device_id);
+  }
+  fclose(f);
+  MaxNodes = (uint64_t)nodes_per_second;
+  totalWorkUnits = threadsX * threadsY;
+  if (totalWorkUnits < 1) totalWorkUnits = 1;
+  return true;
+}
+
+bool engine_alloc(void) {
+  COUNTERS = calloc(totalWorkUnits * 64, sizeof(uint64_t));
+  PV = calloc(MAXPLY, sizeof(uint32_t));
+  GLOBAL_HASHHISTORY = calloc(totalWorkUnits * MAXGAMEPLY, sizeof(uint64_t));
+  RNUMBERS = calloc(totalWorkUnits * 64, sizeof(uint32_t));
+  return COUNTERS && PV && GLOBAL_HASHHISTORY && RNUMBERS;
+}
+
+void engine_free(void) {
+  free(COUNTERS);
+  free(PV);
+  free(GLOBAL_HASHHISTORY);
+  free(RNUMBERS);
+  COUNTERS = NULL;
+  PV = NULL;
+  GLOBAL_HASHHISTORY = NULL;
+  RNUMBERS = NULL;
+}
+
+static void die(void) {
+  cl_release_device();
+  engine_free();
+  exit(EXIT_FAILURE);
+}
+
+void perft(Bitboard *board, int stm, int depth) {
+  ABNODECOUNT = 0;
+  memcpy(GLOBAL_BOARD, board, sizeof GLOBAL_BOARD);
+  memset(COUNTERS, 0, totalWorkUnits * 64 * sizeof(uint64_t));
+  for (uint64_t i = 0; i < totalWorkUnits; i++)
+    memcpy(&GLOBAL_HASHHISTORY[i * MAXGAMEPLY], HashHistory, sizeof HashHistory);
+  if (!cl_write_objects() || !cl_run_perft(stm, depth) || !cl_read_memory()) die();
+  for (uint64_t i = 0; i < totalWorkUnits; i++) ABNODECOUNT += COUNTERS[i * 64 + 1];
+}
+
+/* The 14 known-answer tests of the reference's selftest (src/test.c:43-73). */
+int selftest(void) {
+  static const char *fens[4] = {
+      "rnbqkbnr/pppppppp/8/8/8/8/PPPPPPPP/RNBQKBNR w KQkq -",
+      "8/2p5/3p4/KP5r/1R3p1k/8/4P1P1/8 w - -",
+      "r3k2r/p1ppqpb1/bn2pnp1/3PN3/1p2P3/2N2Q1p/PPPBBPPP/R3K2R w KQkq -",
+      "r4rk1/1pp1qppp/p1np1n2/2b1p1B1/2B1P1b1/P1NP1N2/1PP1QPPP/R4RK1 w - -"};
+  static const struct { int fen, depth; uint64_t count; } kat[14] = {
+      {0, 1, 20}, {0, 2, 400}, {0, 3, 8902}, {0, 4, 197281}, {1, 1, 14}, {1, 2, 191}, {1, 3, 2812},
+      {1, 4, 43238}, {2, 1, 48}, {2, 2, 2039}, {2, 3, 97862}, {3, 1, 46}, {3, 2, 2079}, {3, 3, 89890}};
+  if (!cl_release_device() || !cl_init_device("perft_gpu")) die();
+  int passed = 0;
+  for (int i = 0; i < 14; i++) {
+    Bitboard b[7];
+    int stm, full;
+    printf("#> doing perft depth: %d for position %d of 14\n", kat[i].depth, i + 1);
+    if (!board_setfen(b, &stm, &full, fens[kat[i].fen])) {
+      printf("# Error (in setting fen position): setboard\n");
+      continue;
+    }
+    double t0 = get_time_ms();
+    perft(b, stm, kat[i].depth);
+    double s = (get_time_ms() - t0) / 1000.0 + 1e-9;
+    if (ABNODECOUNT == kat[i].count) {
+      passed++;
+      printf("#> OK, Nodecount Correct, %" PRIu64 " nodes in %lf seconds with %" PRIu64 " nps.\n", ABNODECOUNT, s,
+             (uint64_t)(ABNODECOUNT / s));
+    } else {
+      printf("#> Error, Nodecount NOT Correct, %" PRIu64 " computed nodes != %" PRIu64 " nodes for depth %d.\n",
+             ABNODECOUNT, kat[i].count, kat[i].depth);
+    }
+  }
+  printf("#\n###############################\n### passed %d from 14 tests ###\n###############################\n",
+         passed);
+  if (!cl_release_device() || !cl_init_device("alphabeta_gpu")) die();
+  return passed;
+}
+
+/* Iterative deepening, one launch per depth, the table kept between them
+ * (src/search.c:77-198).  Prints "depth score time nodes pv" lines. */
+Move rootsearch(Bitboard *board, int stm, int depth) {
+  Move best = MOVENONE;
+  int score = 0;
+  double start = get_time_ms();
+  ABNODECOUNT = TTHITS = TTSCOREHITS = IIDHITS = 0;
+  memcpy(GLOBAL_BOARD, board, sizeof GLOBAL_BOARD);
+  for (uint64_t i = 0; i < totalWorkUnits; i++) {
+    memcpy(&GLOBAL_HASHHISTORY[i * MAXGAMEPLY], HashHistory, sizeof HashHistory);
+    for (int j = 0; j < 64; j++) RNUMBERS[i * 64 + j] = (uint32_t)rand();
+  }
+  for (int idf = 1; idf <= depth && idf < MAXPLY; idf++) {
+    memset(COUNTERS, 0, totalWorkUnits * 64 * sizeof(uint64_t));
+    if (!cl_write_objects() || !cl_run_alphabeta(stm, idf, MaxNodes / totalWorkUnits) || !cl_read_memory()) die();
+    for (uint64_t i = 0; i < totalWorkUnits; i++) {
+      ABNODECOUNT += COUNTERS[i * 64 + 1];
+      TTHITS += COUNTERS[i * 64 + 3];
+      TTSCOREHITS += COUNTERS[i * 64 + 4];
+      IIDHITS += COUNTERS[i * 64 + 5];
+    }
+    if (JUSTMOVE(PV[1]) == MOVENONE) break; /* no legal move */
+    best = PV[1];
+    score = (int32_t)PV[0];
+    double el = (get_time_ms() - start) / 1000.0;
+    /* xboard mate scores, src/search.c:131-137 */
+    int xs = score <= -MATESCORE ? -100000 - (INF + score) : score >= MATESCORE ? 100000 - (-INF + score) : score;
+    char mv[6];
+    move2can(best, mv);
+    printf("%d %d %d %" PRIu64 " %s\n", idf, xs, (int)(el * 100), ABNODECOUNT, mv);
+    if (LogFile) fprintf(LogFile, "%d %d %d %" PRIu64 " %s\n", idf, xs, (int)(el * 100), ABNODECOUNT, mv);
+    fflush(stdout);
+    if (score >= MATESCORE || score <= -MATESCORE) break; /* mate found */
+  }
+  return best;
+}

@@ -1,0 +1,130 @@
+/*
+ * xboard.c -- the command loop of the zeta host (src/xboard.c:44-1499):
+ * the CECP/xboard commands a GUI uses to play, plus the console commands
+ * `perft` and `selftest`.  Unknown commands are answered with
+ * "Error (unknown command)" as CECP asks.
+ */
+#include <inttypes.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "../../include/clrun.h"
+#include "engine.h"
+
+static bool xboard_mode = false, force_mode = false, post = true;
+
+static void new_game(void) {
+  int full;
+  board_setfen(BOARD, &STM, &full, "rnbqkbnr/pppppppp/8/8/8/8/PPPPPPPP/RNBQKBNR w KQkq - 0 1");
+  PLY = 0;
+  GAMEPLY = 0;
+  memset(HashHistory, 0, sizeof HashHistory);
+  HashHistory[0] = BOARD[QBBHASH];
+  /* a new game starts from an empty table (src/xboard.c:159-199) */
+  if (!cl_release_device() || !cl_init_device("alphabeta_gpu")) exit(EXIT_FAILURE);
+}
+
+static void play_move(Move m) {
+  board_play(BOARD, STM, m);
+  STM = !STM;
+  PLY++;
+  GAMEPLY++;
+  if (PLY < MAXGAMEPLY) {
+    HashHistory[PLY] = BOARD[QBBHASH];
+    MoveHistory[PLY] = m;
+  }
+}
+
+static void think_and_move(void) {
+  Move m = rootsearch(BOARD, STM, SD);
+  if (JUSTMOVE(m) == MOVENONE) {
+    printf("resign\n");
+    return;
+  }
+  char mv[6];
+  move2can(m, mv);
+  play_move(m);
+  printf("move %s\n", mv);
+  fflush(stdout);
+}
+
+void xboard(void) {
+  char line[4096];
+  new_game();
+  while (fgets(line, sizeof line, stdin)) {
+    char cmd[64] = {0};
+    if (sscanf(line, "%63s", cmd) != 1) continue;
+    const char *arg = line + strlen(cmd);
+    while (*arg == ' ') arg++;
+    if (LogFile) fprintf(LogFile, "> %s", line);
+    if (!strcmp(cmd, "xboard")) {
+      xboard_mode = true;
+      printf("\n");
+    } else if (!strcmp(cmd, "protover")) {
+      printf("feature done=0\nfeature myname=\"Zeta GB300\" ping=1 setboard=1 usermove=1 sigint=0 sigterm=0\n"
+             "feature colors=0 analyze=0 memory=0 reuse=1\nfeature done=1\n");
+    } else if (!strcmp(cmd, "new")) {
+      new_game();
+      force_mode = false;
+      SD = MAXPLY - 1;
+    } else if (!strcmp(cmd, "setboard")) {
+      int full;
+      if (!board_setfen(BOARD, &STM, &full, arg)) printf("tellusererror Illegal position\n");
+      PLY = 0;
+      HashHistory[0] = BOARD[QBBHASH];
+    } else if (!strcmp(cmd, "force")) {
+      force_mode = true;
+    } else if (!strcmp(cmd, "go")) {
+      force_mode = false;
+      think_and_move();
+    } else if (!strcmp(cmd, "usermove")) {
+      char mvs[16] = {0};
+      sscanf(arg, "%15s", mvs);
+      Move m = can2move(mvs, BOARD, STM);
+      play_move(m);
+      if (!force_mode) think_and_move();
+    } else if (!strcmp(cmd, "sd")) {
+      SD = atoi(arg);
+      if (SD < 1) SD = 1;
+      if (SD >= MAXPLY) SD = MAXPLY - 1;
+    } else if (!strcmp(cmd, "ping")) {
+      printf("pong %s", arg);
+    } else if (!strcmp(cmd, "post")) {
+      post = true;
+    } else if (!strcmp(cmd, "nopost")) {
+      post = false;
+    } else if (!strcmp(cmd, "quit")) {
+      break;
+    } else if (!strcmp(cmd, "perft") && !xboard_mode) {
+      int depth = atoi(arg);
+      if (depth < 1) depth = SD < 16 ? SD : 6;
+      printf("### computing perft depth %d: ###\n", depth);
+      if (!cl_release_device() || !cl_init_device("perft_gpu")) exit(EXIT_FAILURE);
+      double t0 = get_time_ms();
+      perft(BOARD, STM, depth);
+      double s = (get_time_ms() - t0 + 1) / 1000.0;
+      printf("nodecount:%" PRIu64 ", seconds: %lf, nps: %" PRIu64 " \n", ABNODECOUNT, s, (uint64_t)(ABNODECOUNT / s));
+      if (!cl_release_device() || !cl_init_device("alphabeta_gpu")) exit(EXIT_FAILURE);
+    } else if (!strcmp(cmd, "selftest") && !xboard_mode) {
+      selftest();
+    } else if (!strcmp(cmd, "print") && !xboard_mode) {
+      char fen[256];
+      board_print(BOARD, STM);
+      board_getfen(BOARD, STM, 1 + PLY / 2, fen, sizeof fen);
+      printf("# %s\n", fen);
+    } else if (!strcmp(cmd, "help") && !xboard_mode) {
+      printf("# commands: new, setboard <fen>, go, usermove <move>, force, sd <depth>, perft <depth>,\n"
+             "# selftest, print, quit (and the xboard protocol)\n");
+    } else if (!strcmp(cmd, "accepted") || !strcmp(cmd, "rejected") || !strcmp(cmd, "level") ||
+               !strcmp(cmd, "st") || !strcmp(cmd, "time") || !strcmp(cmd, "otim") || !strcmp(cmd, "random") ||
+               !strcmp(cmd, "computer") || !strcmp(cmd, "result") || !strcmp(cmd, "hard") ||
+               !strcmp(cmd, "easy") || !strcmp(cmd, "name") || !strcmp(cmd, "rating") || !strcmp(cmd, "white") ||
+               !strcmp(cmd, "black") || !strcmp(cmd, "draw") || !strcmp(cmd, "memory")) {
+      /* accepted and ignored */
+    } else {
+      printf("Error (unknown command): %s\n", cmd);
+    }
+    (void)post;
+    fflush(stdout);
+  }
+}
