@@ -26,6 +26,21 @@ struct __align__(16) Task {
   uint16_t pad;
 };
 
+/* The move-ordering network's ordering of a search node: its 12 best
+ * moves as (from | to << 6); 0xFFFF marks an empty slot (all empty: the
+ * node was requested and is not scored yet). 32 bytes. */
+constexpr int kOrderTop = 12;
+struct OrderEntry {
+  unsigned long long key;
+  uint16_t mv[kOrderTop];
+};
+/* a search node whose ordering the next kernel step computes */
+struct OrderRequest {
+  unsigned long long key;
+  unsigned long long b[5];
+  uint32_t stm, pad;
+};
+
 constexpr int kMaxLevels = 12;   /* split levels per launch: depth <= 15 */
 constexpr int kMaxDepth = 15;
 

@@ -131,6 +131,7 @@ struct SearchOut {
   unsigned long long tthits;
 };
 
+
 /* single out-of-line copies (instruction cache, as in perft.cu) */
 __device__ __noinline__ int s_count(Pos p, int stm, bool *chk) {
   bool c;
@@ -158,7 +159,32 @@ struct Worker {
   unsigned long long nodes, tthits;
   Move killer[kMaxSearchDepth + 1][2];
   int scores[kMaxMoves];
+  /* learned ordering */
+  int learned;
+  OrderEntry *ocache;
+  u64 ocache_mask;
+  OrderRequest *oreq;
+  uint32_t *noreq;
+  uint32_t oreq_cap;
 };
+
+struct LearnArgs {
+  int learned;
+  OrderEntry *cache;
+  u64 mask;
+  OrderRequest *req;
+  uint32_t *nreq;
+  uint32_t cap;
+};
+
+/* rank of move m in a cached network ordering, or -1 */
+__device__ __forceinline__ int learned_rank(const uint16_t *mv, Move m) {
+  const uint16_t k = (uint16_t)(m_from(m) | (m_to(m) << 6));
+#pragma unroll
+  for (int r = 0; r < kOrderTop; r++)
+    if (mv[r] == k) return r;
+  return -1;
+}
 
 /* Set up frame f at `ply`; false when the node is decided on entry (TT
  * hit, busy elsewhere, no legal move), with its value in `value` (kOnEval
@@ -170,8 +196,8 @@ __device__ bool node_enter(Worker &W, Frame &f, int ply, int &value) {
   int ts, td, tb;
   Move tm;
   if (tt_probe(W.tt, W.tt_mask, f.key, ts, td, tb, tm)) {
+    ttm = tm; /* a move from any depth orders; only an equal depth cuts */
     if (td == f.depth) {
-      ttm = tm;
       int s = from_tt(ts, ply);
       if (ply > 0 && (tb == B_EXACT || (tb == B_LOWER && s >= f.beta) || (tb == B_UPPER && s <= f.alpha))) {
         W.tthits++;
@@ -192,11 +218,50 @@ __device__ bool node_enter(Worker &W, Frame &f, int ply, int &value) {
     value = chk ? -kSearchInf + ply : 0;
     return false;
   }
+  /* the network's ordering at nodes with >= 3 plies left: from the cache,
+   * or requested for the next kernel step from nodes with >= 2 left */
+  uint16_t lmv[kOrderTop];
+  bool have_l = false;
+  if (W.learned && f.depth >= 2) {
+    OrderEntry *e = &W.ocache[f.key & W.ocache_mask];
+    const unsigned long long ek = ((volatile unsigned long long *)&e->key)[0];
+    if (ek == f.key) {
+      if (f.depth >= 3) {
+#pragma unroll
+        for (int r = 0; r < kOrderTop; r++) lmv[r] = e->mv[r];
+        have_l = true;
+      }
+    } else {
+      const uint32_t idx = atomicAdd(W.noreq, 1u);
+      if (idx < W.oreq_cap) {
+        OrderRequest q;
+        q.key = f.key;
+        q.b[0] = f.pos.b0;
+        q.b[1] = f.pos.p1;
+        q.b[2] = f.pos.p2;
+        q.b[3] = f.pos.p3;
+        q.b[4] = f.pos.cr;
+        q.stm = f.stm;
+        q.pad = 0;
+        W.oreq[idx] = q;
+        /* mark as requested so other workers do not ask again */
+        OrderEntry pend;
+        pend.key = f.key;
+#pragma unroll
+        for (int r = 0; r < kOrderTop; r++) pend.mv[r] = 0xFFFF;
+        *e = pend;
+      }
+    }
+  }
   /* order once: insertion sort by score, best first */
   const Move k0 = W.killer[ply][0], k1 = W.killer[ply][1];
   for (int i = 0; i < f.n; i++) {
     Move m = f.moves[i];
     int s = order_score(m, f.stm, ttm, k0, k1, *W.T);
+    if (have_l && m != ttm) {
+      const int r = learned_rank(lmv, m);
+      if (r >= 0) s = (1 << 19) - r;
+    }
     int j = i;
     while (j > 0 && W.scores[j - 1] < s) {
       W.scores[j] = W.scores[j - 1];
@@ -229,7 +294,7 @@ __global__ void __launch_bounds__(TPB) k_search_pure(const uint64_t *__restrict_
                                                      int N, int nworkers, int depth, TTEntry *tt, u64 tt_mask,
                                                      uint32_t *busy, u64 busy_mask, uint32_t *done, SearchOut *out,
                                                      unsigned long long budget, uint32_t *status, uint32_t *active,
-                                                     int max_per_pos) {
+                                                     int max_per_pos, LearnArgs la) {
   __shared__ EvalTables sT;
   for (int i = threadIdx.x; i < (int)(sizeof(EvalTables) / 4); i += TPB)
     ((uint32_t *)&sT)[i] = ((const uint32_t *)&kEvalDev)[i];
@@ -245,6 +310,12 @@ __global__ void __launch_bounds__(TPB) k_search_pure(const uint64_t *__restrict_
   W.busy = busy;
   W.busy_mask = busy_mask;
   W.T = &sT;
+  W.learned = la.learned;
+  W.ocache = la.cache;
+  W.ocache_mask = la.mask;
+  W.oreq = la.req;
+  W.noreq = la.nreq;
+  W.oreq_cap = la.cap;
   unsigned long long steps = 0;
 
   /* A worker searches its own position, then helps unfinished ones: it
