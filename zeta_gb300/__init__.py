@@ -101,6 +101,10 @@ SIGNATURES = {
                                        _i32p]),
     "zeta_search": (ctypes.c_int, [_u64p, ctypes.c_int, ctypes.c_int, ctypes.c_int, _u64p, ctypes.c_uint64, _u32p,
                                    _u64p]),
+    "zeta_search_id": (ctypes.c_int, [_u64p, _u8p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _i32p,
+                                      _u32p, _u64p, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float),
+                                      ctypes.POINTER(ctypes.c_float)]),
+    "zeta_search_set_learned_order": (ctypes.c_int, [ctypes.c_int, ctypes.c_int]),
     "zeta_tt_clear": (ctypes.c_int, []),
     "zeta_search_set_helpers": (ctypes.c_int, [ctypes.c_int]),
     "zeta_search_last_ms": (ctypes.c_int, [ctypes.POINTER(ctypes.c_float)]),
@@ -299,6 +303,27 @@ def mlp_scores(boards, stm, fp8: bool = False):
     _check(load_library().zeta_mlp_scores(_ptr(b, _u64p), _ptr(s, _u8p), n, int(fp8), _ptr(sc, _f32p), _ptr(nm, _u8p),
                                           _ptr(best, _i32p)))
     return sc, nm, best
+
+
+def search_id(boards, stm, depth: int, workers: int = 32, ordering: int = 0):
+    """Iterative deepening to `depth`; ordering 0 hand-written, 1 network
+    (BF16), 2 network (FP8).  Returns (scores, moves, nodes, ms_total,
+    ms_search, ms_network)."""
+    b = np.ascontiguousarray(boards, dtype=np.uint64).reshape(-1, 7)
+    s = np.ascontiguousarray(stm, dtype=np.uint8)
+    n = b.shape[0]
+    scores = np.zeros(n, dtype=np.int32)
+    moves = np.zeros(n, dtype=np.uint32)
+    nodes = np.zeros(n, dtype=np.uint64)
+    t = [ctypes.c_float() for _ in range(3)]
+    _check(load_library().zeta_search_id(_ptr(b, _u64p), _ptr(s, _u8p), n, depth, workers, ordering,
+                                         _ptr(scores, _i32p), _ptr(moves, _u32p), _ptr(nodes, _u64p),
+                                         ctypes.byref(t[0]), ctypes.byref(t[1]), ctypes.byref(t[2])))
+    return scores, moves, nodes, t[0].value, t[1].value, t[2].value
+
+
+def search_set_learned_order(top: int = 2, quiet_only: bool = False) -> None:
+    _check(load_library().zeta_search_set_learned_order(top, int(quiet_only)))
 
 
 def tt_clear() -> None:

@@ -135,6 +135,9 @@ int zeta_release(void) {
   cudaFree(c.s_busy);
   cudaFree(c.s_status);
   cudaFree(c.s_tt);
+  cudaFree(c.s_ocache);
+  cudaFree(c.s_oreq);
+  cudaFree(c.s_noreq);
   for (int i = 0; i < 4; i++)
     if (c.ev[i]) cudaEventDestroy(c.ev[i]);
   for (int i = 0; i < 2; i++)
@@ -327,6 +330,23 @@ int zeta_search(const uint64_t board[7], int stm, int depth, int ply_init, const
     memset(counters, 0, 64 * sizeof(uint64_t));
     counters[1] = nodes;
   }
+  return ZETA_OK;
+}
+
+int zeta_search_id(const uint64_t *boards, const uint8_t *stm, int n, int depth, int workers, int ordering,
+                   int32_t *scores, uint32_t *bestmoves, uint64_t *nodes, float *ms_total, float *ms_search,
+                   float *ms_net) {
+  int rc = require_ready();
+  if (rc) return rc;
+  if (!boards || !stm || n <= 0 || depth < 1 || workers < 1 || ordering < 0 || ordering > 2)
+    return set_error(ZETA_ERR_ARG, "bad search arguments");
+  return search_id(boards, stm, n, depth, workers, ordering, scores, bestmoves, nodes, ms_total, ms_search, ms_net);
+}
+
+int zeta_search_set_learned_order(int top, int quiet_only) {
+  if (top < 1 || top > kOrderTop) return set_error(ZETA_ERR_ARG, "learned top must be 1..%d", kOrderTop);
+  g_ctx.s_learned_top = top;
+  g_ctx.s_learned_quiet = quiet_only ? 1 : 0;
   return ZETA_OK;
 }
 

@@ -107,6 +107,13 @@ struct Context {
   uint64_t s_busy_entries = 0;
   uint32_t *s_status = nullptr;
   int s_helpers_cap = 0;      /* max workers per position once helpers join; 0 = no helpers */
+  int s_learned_top = 2;      /* network moves used by the learned ordering */
+  int s_learned_quiet = 0;    /* 1: they order the quiet moves only */
+  void *s_ocache = nullptr;   /* learned ordering: OrderEntry cache */
+  uint64_t s_ocache_entries = 0;
+  void *s_oreq = nullptr;     /* OrderRequest log of the current kernel step */
+  uint32_t *s_noreq = nullptr;
+  uint32_t s_oreq_cap = 0;
   void *s_tt = nullptr;       /* used when zeta_init made no table */
   uint64_t s_tt_entries = 0;
   struct {
@@ -133,7 +140,13 @@ int positions_launch(u64 seed, int n, int min_plies, int max_plies, int min_piec
 int int_peak(double *tops);
 /* search.cu */
 int search_pure_launch(const uint64_t *d_boards, const uint8_t *d_stm, int n, int depth, int workers, int32_t *d_scores,
-                       uint32_t *d_moves, unsigned long long *d_nodes, cudaStream_t s);
+                       uint32_t *d_moves, unsigned long long *d_nodes, cudaStream_t s, int learned = 0);
+int search_id(const uint64_t *boards, const uint8_t *stm, int n, int depth, int workers, int ordering, int32_t *scores,
+              uint32_t *moves, uint64_t *nodes, float *ms_total, float *ms_search, float *ms_mlp);
+/* mlp.cu: score the logged requests and fill the ordering cache */
+int mlp_fill_order_cache(const OrderRequest *req, uint32_t nreq, OrderEntry *cache, uint64_t mask, int fp8,
+                         cudaStream_t s);
+bool mlp_ready_for_search();
 int search_tt_clear(cudaStream_t s);
 /* mlp.cu */
 void mlp_free();

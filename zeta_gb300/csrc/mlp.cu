@@ -599,6 +599,72 @@ int load_data(MlpState &S, const uint64_t *boards, const uint8_t *stm, const uin
   return ZETA_OK;
 }
 
+/* search requests -> board rows for the feature kernel */
+__global__ void k_req_to_boards(const OrderRequest *__restrict__ req, int n, uint64_t *boards, uint8_t *stm) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const OrderRequest q = req[i];
+  uint64_t *b = boards + 7 * (size_t)i;
+  for (int k = 0; k < 5; k++) b[k] = q.b[k];
+  b[5] = q.key;
+  b[6] = 0;
+  stm[i] = (uint8_t)q.stm;
+}
+
+/* the 12 highest-scored moves of each row into the ordering cache, as
+ * real-board (from | to << 6) */
+__global__ void k_topk_cache(const OrderRequest *__restrict__ req, int n, const float *__restrict__ scores,
+                             const uint16_t *__restrict__ moves, const uint8_t *__restrict__ nmoves, OrderEntry *cache,
+                             unsigned long long mask) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int k = nmoves[i];
+  const int flip = req[i].stm ? 56 : 0;
+  float bs[kOrderTop];
+  int bi[kOrderTop];
+#pragma unroll
+  for (int r = 0; r < kOrderTop; r++) {
+    bs[r] = -1e30f;
+    bi[r] = -1;
+  }
+  for (int j = 0; j < k; j++) {
+    float x = scores[(size_t)i * kMaxLegal + j];
+    if (x <= bs[kOrderTop - 1]) continue;
+    int r = kOrderTop - 1;
+    while (r > 0 && bs[r - 1] < x) {
+      bs[r] = bs[r - 1];
+      bi[r] = bi[r - 1];
+      r--;
+    }
+    bs[r] = x;
+    bi[r] = j;
+  }
+  OrderEntry e;
+  e.key = req[i].key;
+#pragma unroll
+  for (int r = 0; r < kOrderTop; r++) {
+    if (bi[r] < 0) {
+      e.mv[r] = 0xFFFF;
+    } else {
+      const uint16_t mv = moves[(size_t)i * kMaxLegal + bi[r]];
+      e.mv[r] = (uint16_t)(((mv & 63) ^ flip) | ((((mv >> 6) & 63) ^ flip) << 6));
+    }
+  }
+  cache[e.key & mask] = e;
+}
+
+int ensure_data(MlpState &S, int n) {
+  if (n <= S.data_cap) return ZETA_OK;
+  cudaFree(S.d_boards);
+  cudaFree(S.d_stm);
+  cudaFree(S.d_targets);
+  S.data_cap = 0;
+  int rc = dalloc(S.d_boards, (size_t)n * 7) | dalloc(S.d_stm, (size_t)n) | dalloc(S.d_targets, (size_t)n);
+  if (rc) return ZETA_ERR_CUDA;
+  S.data_cap = n;
+  return ZETA_OK;
+}
+
 int check_err(MlpState &S, cudaStream_t s) {
   uint32_t e = 0;
   ZCHECK(cudaMemcpyAsync(&e, S.err, 4, cudaMemcpyDeviceToHost, s));
@@ -608,6 +674,29 @@ int check_err(MlpState &S, cudaStream_t s) {
 }
 
 }  // namespace
+
+bool mlp_ready_for_search() { return ctx().mlp && state()->params; }
+
+int mlp_fill_order_cache(const OrderRequest *req, uint32_t nreq, OrderEntry *cache, uint64_t mask, int fp8,
+                         cudaStream_t s) {
+  MlpState &S = *state();
+  const int chunk = 16384;
+  int rc;
+  if ((rc = ensure_rows(S, chunk)) || (rc = ensure_data(S, chunk))) return rc;
+  ZCHECK(cudaMemsetAsync(S.err, 0, 4, s));
+  for (uint32_t off = 0; off < nreq; off += chunk) {
+    const int cnt = (int)(nreq - off < (uint32_t)chunk ? nreq - off : (uint32_t)chunk);
+    const int rows = (cnt + 127) / 128 * 128;
+    k_req_to_boards<<<(cnt + 127) / 128, 128, 0, s>>>(req + off, cnt, S.d_boards, S.d_stm);
+    ZCHECK(cudaGetLastError());
+    if ((rc = forward(S, S.d_boards, S.d_stm, nullptr, cnt, rows, fp8 != 0, s))) return rc;
+    k_head<<<(rows * 32 + 127) / 128, 128, 0, s>>>(S.Q, S.params, S.moves, S.nmoves, S.tidx, rows, 1.f, 0, nullptr,
+                                                   nullptr, nullptr, nullptr, nullptr, S.scores);
+    k_topk_cache<<<(cnt + 127) / 128, 128, 0, s>>>(req + off, cnt, S.scores, S.moves, S.nmoves, cache, mask);
+    ZCHECK(cudaGetLastError());
+  }
+  return check_err(S, s);
+}
 
 void mlp_free() {
   Context &c = ctx();

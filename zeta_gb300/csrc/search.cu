@@ -33,6 +33,8 @@
  *    ZETA_ERR_BUDGET in the status word instead of spinning.
  */
 #include <cstdio>
+#include <cstring>
+#include <vector>
 
 #include "context.cuh"
 #include "eval.cuh"
@@ -160,7 +162,7 @@ struct Worker {
   Move killer[kMaxSearchDepth + 1][2];
   int scores[kMaxMoves];
   /* learned ordering */
-  int learned;
+  int learned, learned_top, learned_quiet;
   OrderEntry *ocache;
   u64 ocache_mask;
   OrderRequest *oreq;
@@ -170,6 +172,8 @@ struct Worker {
 
 struct LearnArgs {
   int learned;
+  int top;   /* how many of the network's best moves are used */
+  int quiet; /* 0: they go right after the TT move; 1: they order the quiet moves only */
   OrderEntry *cache;
   u64 mask;
   OrderRequest *req;
@@ -260,7 +264,12 @@ __device__ bool node_enter(Worker &W, Frame &f, int ply, int &value) {
     int s = order_score(m, f.stm, ttm, k0, k1, *W.T);
     if (have_l && m != ttm) {
       const int r = learned_rank(lmv, m);
-      if (r >= 0) s = (1 << 19) - r;
+      if (r >= 0 && r < W.learned_top) {
+        if (!W.learned_quiet)
+          s = (1 << 19) - r;
+        else if (s < (1 << 16))
+          s = (1 << 15) - r; /* below captures, promotions and killers */
+      }
     }
     int j = i;
     while (j > 0 && W.scores[j - 1] < s) {
@@ -311,6 +320,8 @@ __global__ void __launch_bounds__(TPB) k_search_pure(const uint64_t *__restrict_
   W.busy_mask = busy_mask;
   W.T = &sT;
   W.learned = la.learned;
+  W.learned_top = la.top;
+  W.learned_quiet = la.quiet;
   W.ocache = la.cache;
   W.ocache_mask = la.mask;
   W.oreq = la.req;
@@ -496,9 +507,31 @@ int search_tt_clear(cudaStream_t s) {
   return ZETA_OK;
 }
 
-int search_pure_launch(const uint64_t *d_boards, const uint8_t *d_stm, int n, int depth, int workers, int32_t *d_scores,
-                       uint32_t *d_moves, unsigned long long *d_nodes, cudaStream_t s) {
+/* ordering cache and request log of the learned ordering */
+static int learn_buffers() {
   Context &c = ctx();
+  if (!c.s_ocache) {
+    c.s_ocache_entries = 1ull << 22; /* 128 MiB of 32-byte entries */
+    ZCHECK(cudaMalloc(&c.s_ocache, c.s_ocache_entries * sizeof(OrderEntry)));
+    ZCHECK(cudaMemset(c.s_ocache, 0, c.s_ocache_entries * sizeof(OrderEntry)));
+    c.s_oreq_cap = 1u << 20;
+    ZCHECK(cudaMalloc(&c.s_oreq, (size_t)c.s_oreq_cap * sizeof(OrderRequest)));
+    ZCHECK(cudaMalloc(&c.s_noreq, sizeof(uint32_t)));
+    ZCHECK(cudaMemset(c.s_noreq, 0, sizeof(uint32_t)));
+  }
+  return ZETA_OK;
+}
+
+int search_pure_launch(const uint64_t *d_boards, const uint8_t *d_stm, int n, int depth, int workers, int32_t *d_scores,
+                       uint32_t *d_moves, unsigned long long *d_nodes, cudaStream_t s, int learned) {
+  Context &c = ctx();
+  LearnArgs la{0, 0, 0, nullptr, 0, nullptr, nullptr, 0};
+  if (learned) {
+    int rc = learn_buffers();
+    if (rc) return rc;
+    la = LearnArgs{1, c.s_learned_top, c.s_learned_quiet, (OrderEntry *)c.s_ocache, c.s_ocache_entries - 1, (OrderRequest *)c.s_oreq,
+                   c.s_noreq, c.s_oreq_cap};
+  }
   if (n <= 0 || workers <= 0 || depth < 1 || depth > kMaxSearchDepth - 1)
     return set_error(ZETA_ERR_ARG, "search: need n > 0, workers > 0, depth 1..%d", kMaxSearchDepth - 1);
   if ((long long)n * workers > (1ll << 31)) return set_error(ZETA_ERR_ARG, "search: too many workers");
@@ -516,7 +549,7 @@ int search_pure_launch(const uint64_t *d_boards, const uint8_t *d_stm, int n, in
   ZCHECK(cudaEventRecord(c.ev[1], s));
   k_search_pure<128><<<(unsigned)((threads + tpb - 1) / tpb), tpb, 0, s>>>(
       d_boards, d_stm, n, workers, depth, tt, entries - 1, c.s_busy, c.s_busy_entries - 1, c.s_done,
-      (SearchOut *)c.s_out, budget, c.s_status, c.s_done + n, c.s_helpers_cap);
+      (SearchOut *)c.s_out, budget, c.s_status, c.s_done + n, c.s_helpers_cap, la);
   ZCHECK(cudaGetLastError());
   ZCHECK(cudaEventRecord(c.ev[2], s));
   k_search_scatter<<<(n + 127) / 128, 128, 0, s>>>((const SearchOut *)c.s_out, n, d_scores, d_moves, d_nodes);
@@ -530,6 +563,97 @@ int search_pure_launch(const uint64_t *d_boards, const uint8_t *d_stm, int n, in
   c.sstats.kernel_ms = ms;
   if (status & SST_BUDGET) return set_error(ZETA_ERR_BUDGET, "search: a worker ran out of its node budget");
   return ZETA_OK;
+}
+
+/* Iterative deepening 1..depth over a batch, the transposition table
+ * kept between iterations (src/search.c:77-198 does the same per launch).
+ * With ordering > 0 every iteration is one kernel step of the learned
+ * ordering: the search logs the nodes that have no network ordering yet,
+ * then one batched tensor-core inference (BF16, or FP8 when ordering == 2)
+ * scores them all and the next iteration orders by the result.  Host
+ * outputs: final scores and best moves, nodes summed over all iterations,
+ * wall time, search-kernel time and network time (ms). */
+int search_id(const uint64_t *boards, const uint8_t *stm, int n, int depth, int workers, int ordering, int32_t *scores,
+              uint32_t *moves, uint64_t *nodes, float *ms_total, float *ms_search, float *ms_mlp) {
+  Context &c = ctx();
+  const int learned = ordering > 0;
+  if (learned && !mlp_ready_for_search())
+    return set_error(ZETA_ERR_STATE, "learned ordering needs zeta_mlp_init (and training or parameters)");
+  cudaStream_t s = c.stream;
+  uint64_t *db = nullptr, *dn = nullptr;
+  uint8_t *ds = nullptr;
+  int32_t *dsc = nullptr;
+  uint32_t *dm = nullptr;
+  cudaError_t e = cudaMalloc(&db, (size_t)n * 56);
+  if (e == cudaSuccess) e = cudaMalloc(&ds, n);
+  if (e == cudaSuccess) e = cudaMalloc(&dsc, (size_t)n * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&dm, (size_t)n * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&dn, (size_t)n * 8);
+  if (e == cudaSuccess) e = cudaMemcpy(db, boards, (size_t)n * 56, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(ds, stm, n, cudaMemcpyHostToDevice);
+  int rc = e == cudaSuccess ? ZETA_OK : cuda_fail(e, "search_id buffers");
+  if (!rc && learned) rc = learn_buffers();
+  if (!rc && learned) {
+    e = cudaMemsetAsync(c.s_ocache, 0, c.s_ocache_entries * sizeof(OrderEntry), s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c.s_noreq, 0, 4, s);
+    if (e != cudaSuccess) rc = cuda_fail(e, "search_id cache");
+  }
+  std::vector<uint64_t> it(n);
+  if (nodes) memset(nodes, 0, (size_t)n * 8);
+  float t_search = 0.f, t_mlp = 0.f;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventRecord(e0, s);
+  for (int d = 1; d <= depth && !rc; d++) {
+    rc = search_pure_launch(db, ds, n, d, workers, dsc, dm, (unsigned long long *)dn, s, learned);
+    if (rc) break;
+    t_search += c.sstats.kernel_ms;
+    if (cudaMemcpy(it.data(), dn, (size_t)n * 8, cudaMemcpyDeviceToHost) != cudaSuccess) {
+      rc = set_error(ZETA_ERR_CUDA, "search_id read-back");
+      break;
+    }
+    if (nodes)
+      for (int i = 0; i < n; i++) nodes[i] += it[i];
+    if (learned && d < depth) {
+      uint32_t nreq = 0;
+      cudaMemcpy(&nreq, c.s_noreq, 4, cudaMemcpyDeviceToHost);
+      if (nreq > c.s_oreq_cap) nreq = c.s_oreq_cap;
+      cudaEvent_t m0, m1;
+      cudaEventCreate(&m0);
+      cudaEventCreate(&m1);
+      cudaEventRecord(m0, s);
+      if (nreq) rc = mlp_fill_order_cache((const OrderRequest *)c.s_oreq, nreq, (OrderEntry *)c.s_ocache,
+                                          c.s_ocache_entries - 1, ordering == 2, s);
+      cudaEventRecord(m1, s);
+      cudaEventSynchronize(m1);
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, m0, m1);
+      t_mlp += ms;
+      cudaEventDestroy(m0);
+      cudaEventDestroy(m1);
+      cudaMemsetAsync(c.s_noreq, 0, 4, s);
+    }
+  }
+  cudaEventRecord(e1, s);
+  cudaEventSynchronize(e1);
+  float tot = 0.f;
+  cudaEventElapsedTime(&tot, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (!rc) {
+    if (scores) cudaMemcpy(scores, dsc, (size_t)n * 4, cudaMemcpyDeviceToHost);
+    if (moves) cudaMemcpy(moves, dm, (size_t)n * 4, cudaMemcpyDeviceToHost);
+  }
+  cudaFree(db);
+  cudaFree(ds);
+  cudaFree(dsc);
+  cudaFree(dm);
+  cudaFree(dn);
+  if (ms_total) *ms_total = tot;
+  if (ms_search) *ms_search = t_search;
+  if (ms_mlp) *ms_mlp = t_mlp;
+  return rc;
 }
 
 }  // namespace zeta
