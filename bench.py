@@ -364,6 +364,80 @@ def run_search(args):
     z.release()
 
 
+GEMM_SHAPES = (
+    # (M, N, K): the move-ordering network's layers at a 65536-position batch
+    (65536, 512, 768),   # forward layer 1 (768 one-hot -> 512)
+    (65536, 256, 512),   # forward layer 2
+    (65536, 128, 256),   # head (q_from, q_to)
+    (768, 512, 65536),   # weight gradient of layer 1 (K = positions)
+    (8192, 8192, 8192),  # square, the shape of the measured bf16 peak
+)
+
+
+def run_gemm(args):
+    """The tensor-core GEMM (zeta_gemm_tc, tcgen05.mma, FP32 accumulation)
+    on the network's shapes, BF16 and FP8, next to torch.matmul (cuBLAS) on
+    the same BF16 operands.  Metric: TFLOP/s (2*M*N*K per product)."""
+    import torch
+    import zeta_gb300 as z
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    z.init(local, 0, 0)
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
+    g = torch.Generator(device=dev).manual_seed(7)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device=dev)
+    peaks = measured_peaks()
+    rows = []
+    for (M, N, K) in GEMM_SHAPES:
+        A = (torch.rand(M, K, device=dev, generator=g) - 0.5).to(torch.bfloat16)
+        B = (torch.rand(N, K, device=dev, generator=g) - 0.5).to(torch.bfloat16)
+        C = torch.empty(M, N, device=dev, dtype=torch.float32)
+        A8, B8 = A.to(torch.float8_e4m3fn), B.to(torch.float8_e4m3fn)
+        flops = 2.0 * M * N * K
+        res = {"M": M, "N": N, "K": K}
+        for name, fn in (("bf16", lambda: z.gemm_tc(A.data_ptr(), B.data_ptr(), C.data_ptr(), M, N, K, False,
+                                                     stream.cuda_stream)),
+                         ("fp8", lambda: z.gemm_tc(A8.data_ptr(), B8.data_ptr(), C.data_ptr(), M, N, K, True,
+                                                    stream.cuda_stream)),
+                         ("cublas_bf16", lambda: torch.matmul(A, B.t()))):
+            for _ in range(args.warmup):
+                fn()
+            ms = []
+            for _ in range(args.steps):
+                flush.fill_(1)
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                fn()
+                e1.record(stream)
+                e1.synchronize()
+                ms.append(e0.elapsed_time(e1))
+            t = statistics.median(ms)
+            res[name] = {"ms": round(t, 4), "tflops": round(flops / t / 1e9, 1)}
+        ref = (A.float() @ B.float().t())
+        z.gemm_tc(A.data_ptr(), B.data_ptr(), C.data_ptr(), M, N, K, False, stream.cuda_stream)
+        res["bf16_max_rel_err"] = float(((C - ref).abs().max() / ref.abs().max()).item())
+        rows.append(res)
+        print(json.dumps(res), file=sys.stderr, flush=True)
+        del A, B, C, A8, B8, ref
+    if rank == 0:
+        head = rows[0]
+        peak = peaks.get("bf16_tflops") or 1900.0
+        print(json.dumps({
+            "metric": "tensor-core GEMM TFLOP/s (move-ordering network, layer 1)", "value": head["bf16"]["tflops"],
+            "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": head["bf16"]["ms"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "bf16 (fp32 accumulate)", "data": "synthetic (uniform operands)",
+            "config": {"workload": "zeta_gemm_tc on the network's shapes", "l2": "flushed between timed steps"},
+            "roofline": {"bound": "tensor", "achieved": head["bf16"]["tflops"], "peak": peak, "unit": "TFLOP/s",
+                         "frac": round(head["bf16"]["tflops"] / peak, 4), "traffic": None,
+                         "peak_source": "MEASURED_PEAKS.json bf16_tflops (cuBLAS burst)"},
+            "shapes": rows,
+        }), flush=True)
+    z.release()
+
+
 def run_reference(args):
     world, rank, _ = dist_env()
     if rank != 0:
@@ -412,7 +486,7 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--n", type=int, default=0, help="positions per GPU (default: the workload's 4096)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the timed CPU baseline (profiling runs)")
-    ap.add_argument("--workload", choices=["perft_batch", "search_batch"], default="perft_batch")
+    ap.add_argument("--workload", choices=["perft_batch", "search_batch", "gemm"], default="perft_batch")
     ap.add_argument("--depth", type=int, default=0, help="search depth (search_batch; default 7)")
     ap.add_argument("--workers", type=int, default=0, help="ABDADA workers per position (0 = sweep)")
     ap.add_argument("--helpers", type=int, default=0, help="helper cap: max workers per position (0 = none)")
@@ -421,6 +495,8 @@ def main():
         args.warmup = 3
     if args.workload == "search_batch" and args.impl == "ours":
         run_search(args)
+    elif args.workload == "gemm" and args.impl == "ours":
+        run_gemm(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -151,10 +151,11 @@ int zeta_search_id(const uint64_t *boards, const uint8_t *stm, int n, int depth,
                    int32_t *scores, uint32_t *bestmoves, uint64_t *nodes, float *ms_total, float *ms_search,
                    float *ms_net);
 /* How the network's ordering enters the move order: its `top` best moves
- * (1..12, default 2) are searched right after the transposition-table move
- * (quiet_only = 0, the default), or they order only the quiet moves, after
- * the captures, promotions and killers (quiet_only = 1).  The other moves
- * keep the hand-written order. */
+ * (1..12) are searched right after the transposition-table move
+ * (quiet_only = 0), or they order only the quiet moves, after the
+ * captures, promotions and killers (quiet_only = 1).  The other moves keep
+ * the hand-written order.  Default: top 12, quiet_only 1 (the setting that
+ * visits fewer nodes than the hand-written ordering). */
 int zeta_search_set_learned_order(int top, int quiet_only);
 /* Workers that finish their own position help unfinished ones, up to this
  * many workers per position (0, the default: no helping). */

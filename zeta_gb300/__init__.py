@@ -322,7 +322,7 @@ def search_id(boards, stm, depth: int, workers: int = 32, ordering: int = 0):
     return scores, moves, nodes, t[0].value, t[1].value, t[2].value
 
 
-def search_set_learned_order(top: int = 2, quiet_only: bool = False) -> None:
+def search_set_learned_order(top: int = 12, quiet_only: bool = True) -> None:
     _check(load_library().zeta_search_set_learned_order(top, int(quiet_only)))
 
 

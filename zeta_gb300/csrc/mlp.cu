@@ -183,8 +183,8 @@ using namespace zeta;
  * when a tensor-core wait timed out. */
 extern "C" int zeta_gemm_tc(const void *d_A, const void *d_B, float *d_C, int M, int N, int K, int fp8, void *stream) {
   if (!d_A || !d_B || !d_C) return set_error(ZETA_ERR_ARG, "null buffer");
-  uint32_t *d_err = nullptr;
-  ZCHECK(cudaMalloc(&d_err, 4));
+  static uint32_t *d_err = nullptr; /* one error word, kept for the process */
+  if (!d_err) ZCHECK(cudaMalloc(&d_err, 4));
   cudaStream_t s = (cudaStream_t)stream;
   ZCHECK(cudaMemsetAsync(d_err, 0, 4, s));
   GemmArgs g{d_A, d_B, M, N, K, nullptr, 0, d_C, nullptr, nullptr, 1.f, d_err, nullptr, nullptr, nullptr};
@@ -195,7 +195,6 @@ extern "C" int zeta_gemm_tc(const void *d_A, const void *d_B, float *d_C, int M,
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) rc = cuda_fail(e, "zeta_gemm_tc");
   }
-  cudaFree(d_err);
   if (rc) return rc;
   if (err) return set_error(ZETA_ERR_BUDGET, "gemm: tensor-core wait timed out");
   return ZETA_OK;

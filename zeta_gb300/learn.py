@@ -67,7 +67,7 @@ def load(z, path: str = MODEL) -> bool:
     return True
 
 
-def ab_test(z, boards, stm, depth: int, workers: int = 32, orderings=((0, 2, 0), (1, 2, 0), (2, 2, 0))):
+def ab_test(z, boards, stm, depth: int, workers: int = 32, orderings=((0, 12, 1), (1, 12, 1), (2, 12, 1))):
     """Iterative deepening to `depth` under each (ordering, top, quiet_only)
     from a cleared table each time.  Returns per-case scores, nodes and
     times, keyed "plain" or "bf16/fp8-top<k>[-quiet]"."""
@@ -79,7 +79,7 @@ def ab_test(z, boards, stm, depth: int, workers: int = 32, orderings=((0, 2, 0),
         key = "plain" if o == 0 else f"{'bf16' if o == 1 else 'fp8'}-top{top}{'-quiet' if quiet else ''}"
         out[key] = {"scores": sc, "moves": mv, "nodes": int(nodes.sum()), "ms_total": ms, "ms_search": ms_s,
                     "ms_network": ms_n}
-    z.search_set_learned_order(2, False)
+    z.search_set_learned_order(12, True)
     return out
 
 
@@ -93,7 +93,7 @@ def main():
     ap.add_argument("--depth", type=int, default=8)
     ap.add_argument("--workers", type=int, default=32)
     ap.add_argument("--out", default="")
-    ap.add_argument("--cases", default="0:2:0,1:2:0,2:2:0",
+    ap.add_argument("--cases", default="0:12:1,1:12:1,2:12:1",
                     help="comma-separated ordering:top:quiet_only cases of the A/B")
     a = ap.parse_args()
     z.init(0, 1024, 0)
