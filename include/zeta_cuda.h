@@ -71,7 +71,7 @@ int zeta_perft_batch_device(const uint64_t *d_boards, const uint8_t *d_stm, cons
  * their own pool or budget, and latency-critical loops where a cudaMalloc
  * (which may synchronise the device) is not allowed.  No counterpart in
  * the reference.  It calls no cudaMalloc/cudaFree and needs no zeta_init:
- * its scratch is one fixed device array of about 19 MB inside the library,
+ * its scratch is one fixed device array of about 29 MB inside the library,
  * held by every GPU that loads it until the process exits.
  *  - Limits: n <= 131072 positions, and the tree split may make at most
  *    131072 subtree tasks per level; beyond either it returns
