@@ -166,6 +166,34 @@ int zeta_tt_clear(void);
 int zeta_search_last_ms(float *kernel_ms);
 
 /* ------------------------------------------------------------------ */
+/* Full-engine search: the reference's alphabeta_gpu (zeta.cl:852-2511)
+ * with its heuristics -- quiescence with stand pat, check and promotion
+ * extensions, null move (R=2), late move reductions (R=1) with re-search,
+ * internal iterative deepening, TT / IID / killer / counter-move ordering,
+ * repetition, fifty-move and bare-kings draws, TT1 with the reference's
+ * replacement and aging, ABDADA TT2 locks between workers, PV from TT1.
+ * One worker searches exactly the reference's tree (same score, PV and
+ * node count); more workers share the tables as the reference's
+ * work-groups do.  TT1 / TT2 (zeta_init), killer and counter moves persist
+ * between calls until zeta_tt_clear, as the reference's device buffers do.
+ *
+ * One launch: cl_run_alphabeta + cl_read_memory (src/clrun.c:675-974,
+ * 1150-1266).  hash_history: MAXGAMEPLY (1024) hashes of the game, entry
+ * ply_init = this position (NULL: the root hash only); max_nodes stops the
+ * search when worker 0 has made more moves (the reference's COUNTERS[1]
+ * test).  pv: PV[0] score, PV[1..63] moves, zero when the search was
+ * stopped; counters: workers x 64, slot 1 nodes, 3 TT-move hits, 4
+ * TT-score hits, 5 IID-move hits (src/search.c:111-117). */
+int zeta_engine_search(const uint64_t board[7], int stm, int depth, int ply_init, const uint64_t *hash_history,
+                       uint64_t max_nodes, int workers, uint32_t pv[64], uint64_t *counters);
+/* n positions in one launch, `workers` each; each position searches with a
+ * power-of-two slice (1/n) of TT1 and TT2, ply_init 0.  Outputs per
+ * position: score, best move (0 if stopped), nodes summed over workers,
+ * and the PV (n x 64, may be NULL). */
+int zeta_engine_batch(const uint64_t *boards, const uint8_t *stm, int n, int depth, int workers, uint64_t max_nodes,
+                      int32_t *scores, uint32_t *bestmoves, uint64_t *nodes, uint32_t *pvs);
+
+/* ------------------------------------------------------------------ */
 /* The move-ordering network (no counterpart in the reference): 768
  * one-hot inputs -> 512 -> 256 ReLU -> (q_from, q_to); a move scores
  * q_from . E_from[from] + q_to . E_to[to].  Trained with Adam on the

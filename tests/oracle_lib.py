@@ -94,6 +94,43 @@ def ref_perft_batch(boards, stm, depth, threads: int) -> np.ndarray:
     return out
 
 
+class RefSearch:
+    """The reference's alphabeta_gpu kernel on the host (refshim), with its
+    own transposition tables, killer and counter moves kept between runs as
+    the reference keeps its device buffers (src/clrun.c:387-511)."""
+
+    def __init__(self, tt1_entries: int, tt2_entries: int, workers: int = 1):
+        self.r = reference()
+        if self.r is None:
+            raise RuntimeError("reference kernels not built")
+        self.workers = workers
+        self.h = self.r.ref_search_new(tt1_entries, tt2_entries, workers)
+
+    def run(self, board, stm: int, depth: int, ply_init: int = 0, hist=None, max_nodes: int = 1 << 40):
+        """One cl_run_alphabeta launch: (PV uint32[64], counters uint64[workers, 64])."""
+        b = _b7(board)
+        h = np.zeros(1024, dtype=np.uint64)
+        if hist is None:
+            h[ply_init] = np.uint64(int(np.asarray(board, dtype=np.uint64).reshape(7)[5]))
+        else:
+            h[:] = np.asarray(hist, dtype=np.uint64).reshape(1024)
+        pv = np.zeros(64, dtype=np.uint32)
+        cnt = np.zeros((self.workers, 64), dtype=np.uint64)
+        self.r.ref_search_run(self.h, b, int(stm), int(depth), int(ply_init),
+                              h.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)), None, max_nodes,
+                              pv.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)),
+                              cnt.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)))
+        return pv, cnt
+
+    def clear(self):
+        self.r.ref_search_clear(self.h)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.r.ref_search_free(self.h)
+            self.h = None
+
+
 def genmoves(board, stm: int, qs: bool = False) -> list[int]:
     buf = (ctypes.c_uint32 * 256)()
     n = oracle().zo_genmoves(_b7(board), int(stm), int(qs), buf)
@@ -163,6 +200,10 @@ def playout(seed: int, plies: int):
     stm = ctypes.c_int()
     ok = oracle().zo_playout(ctypes.c_uint64(seed & (2**64 - 1)), plies, b, ctypes.byref(stm))
     return (np.array(list(b), dtype=np.uint64), stm.value) if ok else None
+
+
+def can2move(board, stm: int, can: str) -> int:
+    return int(oracle().zo_can2move(can.encode(), _b7(board), int(stm)))
 
 
 def move2can(move: int) -> str:

@@ -84,6 +84,10 @@ SIGNATURES = {
                                            ctypes.c_int, ctypes.c_int, _u64p, _u8p, _u8p]),
     "zeta_int_peak": (ctypes.c_int, [ctypes.POINTER(ctypes.c_double)]),
     "zeta_search_batch": (ctypes.c_int, [_u64p, _u8p, ctypes.c_int, ctypes.c_int, ctypes.c_int, _i32p, _u32p, _u64p]),
+    "zeta_engine_search": (ctypes.c_int, [_u64p, ctypes.c_int, ctypes.c_int, ctypes.c_int, _u64p, ctypes.c_uint64,
+                                          ctypes.c_int, _u32p, _u64p]),
+    "zeta_engine_batch": (ctypes.c_int, [_u64p, _u8p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_uint64,
+                                         _i32p, _u32p, _u64p, _u32p]),
     "zeta_search_batch_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
                                                 ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                                 ctypes.c_void_p]),
@@ -320,6 +324,35 @@ def search_id(boards, stm, depth: int, workers: int = 32, ordering: int = 0):
                                          _ptr(scores, _i32p), _ptr(moves, _u32p), _ptr(nodes, _u64p),
                                          ctypes.byref(t[0]), ctypes.byref(t[1]), ctypes.byref(t[2])))
     return scores, moves, nodes, t[0].value, t[1].value, t[2].value
+
+
+def engine_search(board, stm: int, depth: int, workers: int = 1, ply_init: int = 0, hash_history=None,
+                  max_nodes: int = (1 << 63)):
+    """One full-engine search launch: (pv uint32[64], counters uint64[workers, 64])."""
+    b = np.ascontiguousarray(board, dtype=np.uint64).reshape(7)
+    h = None if hash_history is None else np.ascontiguousarray(hash_history, dtype=np.uint64).reshape(1024)
+    pv = np.zeros(64, dtype=np.uint32)
+    cnt = np.zeros((workers, 64), dtype=np.uint64)
+    _check(load_library().zeta_engine_search(_ptr(b, _u64p), int(stm), depth, ply_init,
+                                             _ptr(h, _u64p) if h is not None else None, max_nodes, workers,
+                                             _ptr(pv, _u32p), _ptr(cnt, _u64p)))
+    return pv, cnt
+
+
+def engine_batch(boards, stm, depth: int, workers: int = 1, max_nodes: int = (1 << 63), with_pv: bool = False):
+    """Full-engine search of n positions in one launch: (scores, best moves,
+    nodes[, pvs n x 64])."""
+    b = np.ascontiguousarray(boards, dtype=np.uint64).reshape(-1, 7)
+    s = np.ascontiguousarray(stm, dtype=np.uint8)
+    n = b.shape[0]
+    scores = np.zeros(n, dtype=np.int32)
+    moves = np.zeros(n, dtype=np.uint32)
+    nodes = np.zeros(n, dtype=np.uint64)
+    pvs = np.zeros((n, 64), dtype=np.uint32) if with_pv else None
+    _check(load_library().zeta_engine_batch(_ptr(b, _u64p), _ptr(s, _u8p), n, depth, workers, max_nodes,
+                                            _ptr(scores, _i32p), _ptr(moves, _u32p), _ptr(nodes, _u64p),
+                                            _ptr(pvs, _u32p) if with_pv else None))
+    return (scores, moves, nodes, pvs) if with_pv else (scores, moves, nodes)
 
 
 def search_set_learned_order(top: int = 12, quiet_only: bool = True) -> None:

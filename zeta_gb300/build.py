@@ -29,7 +29,7 @@ REFERENCE_SRC = "/root/reference/src"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"] + ARCH
 
-CUDA_SOURCES = ["capi.cu", "perft.cu", "positions.cu", "peak.cu", "search.cu"]
+CUDA_SOURCES = ["capi.cu", "perft.cu", "positions.cu", "peak.cu", "search.cu", "engine.cu"]
 OPTIONAL_CUDA_SOURCES = ["search.cu", "mlp.cu", "noalloc.cu"]
 HOST_SOURCES = ["board.c", "cudarun.c", "engine.c", "xboard.c", "main.c"]
 

@@ -117,6 +117,7 @@ int zeta_release(void) {
   if (!c.ready) return ZETA_OK;
   if (c.graph) cudaGraphExecDestroy(c.graph);
   mlp_free();
+  engine_free();
   cudaFree(c.lvl[0]);
   cudaFree(c.lvl[1]);
   cudaFree(c.fin);
@@ -360,6 +361,8 @@ int zeta_tt_clear(void) {
   int rc = require_ready();
   if (rc) return rc;
   rc = search_tt_clear(g_ctx.stream);
+  if (rc) return rc;
+  rc = engine_clear(g_ctx.stream);
   if (rc) return rc;
   ZCHECK(cudaStreamSynchronize(g_ctx.stream));
   return ZETA_OK;

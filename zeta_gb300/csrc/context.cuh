@@ -96,6 +96,7 @@ struct Context {
 
   /* transposition tables (search) */
   void *mlp = nullptr; /* move-ordering network state (mlp.cu) */
+  int tt_owner = 0;    /* entry format held in tt1: 1 pure search, 2 full engine */
   void *tt1 = nullptr, *tt2 = nullptr;
   uint64_t tt1_entries = 0, tt2_entries = 0;
 
@@ -150,6 +151,9 @@ bool mlp_ready_for_search();
 int search_tt_clear(cudaStream_t s);
 /* mlp.cu */
 void mlp_free();
+/* engine.cu: the full-engine search */
+int engine_clear(cudaStream_t s);
+void engine_free();
 int genmoves_launch(const uint64_t *d_boards, const uint8_t *d_stm, int n, int qs, uint32_t *d_moves,
                     int32_t *d_counts, cudaStream_t stream);
 

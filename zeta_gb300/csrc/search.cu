@@ -537,6 +537,11 @@ int search_pure_launch(const uint64_t *d_boards, const uint8_t *d_stm, int n, in
   if ((long long)n * workers > (1ll << 31)) return set_error(ZETA_ERR_ARG, "search: too many workers");
   int rc = search_buffers(n);
   if (rc) return rc;
+  if (c.tt_owner != 1 && c.tt1) {
+    /* the full engine keeps a different entry format in the same table */
+    ZCHECK(cudaMemsetAsync(c.tt1, 0, c.tt1_entries * 16, s));
+  }
+  c.tt_owner = 1;
   TTEntry *tt = (TTEntry *)(c.tt1 ? c.tt1 : c.s_tt);
   u64 entries = c.tt1 ? c.tt1_entries : c.s_tt_entries;
   ZCHECK(cudaMemsetAsync(c.s_out, 0, (size_t)n * sizeof(SearchOut), s));
