@@ -364,6 +364,59 @@ def run_search(args):
     z.release()
 
 
+def run_engine(args):
+    """Full-engine search (the reference's heuristics): 256 seeded playout
+    positions (20-40 plies, >= 20 pieces), iterative deepening to a depth
+    with ABDADA workers per position, 8 GB TT1 + 2 GB TT2 split evenly over
+    the positions; plain ordering vs the move-ordering network (BF16).
+    Metric: positions per second to the depth (time-to-depth of the batch)."""
+    import torch
+    import zeta_gb300 as z
+    from zeta_gb300 import learn
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    z.init(local, 8192, 2048)
+    w = dict(z.WORKLOADS["engine"])
+    n = args.n or 256
+    boards, stm, _ = z.make_positions(w["seed"] + 0x1000003 * rank, n, w["min_plies"], w["max_plies"],
+                                      w["min_pieces"], 0, 0)
+    depth = args.depth or 8
+    workers = args.workers or 16
+    have_net = learn.load(z)
+    cases = [0] + ([1] if have_net else [])
+    z.engine_id(boards[:32], stm[:32], min(depth, 5), workers, 0)  # warm-up (buffers, code)
+    res = {}
+    with ClockSampler(local) as clocks:
+        for o in cases:
+            sc, mv, nodes, dd, ms, ms_s, ms_n = z.engine_id(boards, stm, depth, workers, o)
+            res[o] = {"scores": sc, "moves": mv, "nodes": int(nodes.sum()), "ms_total": ms, "ms_search": ms_s,
+                      "ms_network": ms_n, "depth_min": int(dd.min())}
+            print(json.dumps({"ordering": o, "nodes": res[o]["nodes"], "ms_total": round(ms, 2),
+                              "ms_network": round(ms_n, 2), "depth_min": res[o]["depth_min"]}), file=sys.stderr,
+                  flush=True)
+    p = res[0]
+    line = {
+        "metric": f"full-engine search positions/s to depth {depth} (reference heuristics)",
+        "value": round(n / (p["ms_total"] / 1e3), 3), "unit": "positions/s", "n_gpus": world, "steps": 1,
+        "warmup": 1, "ms_per_step": round(p["ms_total"], 2), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded random playouts)",
+        "config": {"workload": f"engine: {n} playouts of 20-40 plies, >=20 pieces, iterative deepening 1..{depth}",
+                   "workers_per_position": workers, "tt": "8 GB TT1 + 2 GB TT2, 1/n per position"},
+        "nodes_per_s": round(p["nodes"] / (p["ms_total"] / 1e3), 1), "nodes": p["nodes"],
+        "clocks": clocks.summary(),
+    }
+    if 1 in res:
+        l1 = res[1]
+        line["learned_bf16"] = {
+            "ms_total": round(l1["ms_total"], 2), "ms_network": round(l1["ms_network"], 2), "nodes": l1["nodes"],
+            "time_to_depth_ratio": round(l1["ms_total"] / p["ms_total"], 4),
+            "score_agreement": round(float((l1["scores"] == p["scores"]).mean()), 4),
+            "best_move_agreement": round(float((l1["moves"] == p["moves"]).mean()), 4)}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    z.release()
+
+
 GEMM_SHAPES = (
     # (M, N, K): the move-ordering network's layers at a 65536-position batch
     (65536, 512, 768),   # forward layer 1 (768 one-hot -> 512)
@@ -486,7 +539,7 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--n", type=int, default=0, help="positions per GPU (default: the workload's 4096)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the timed CPU baseline (profiling runs)")
-    ap.add_argument("--workload", choices=["perft_batch", "search_batch", "gemm"], default="perft_batch")
+    ap.add_argument("--workload", choices=["perft_batch", "search_batch", "gemm", "engine"], default="perft_batch")
     ap.add_argument("--depth", type=int, default=0, help="search depth (search_batch; default 7)")
     ap.add_argument("--workers", type=int, default=0, help="ABDADA workers per position (0 = sweep)")
     ap.add_argument("--helpers", type=int, default=0, help="helper cap: max workers per position (0 = none)")
@@ -497,6 +550,8 @@ def main():
         run_search(args)
     elif args.workload == "gemm" and args.impl == "ours":
         run_gemm(args)
+    elif args.workload == "engine" and args.impl == "ours":
+        run_engine(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -192,6 +192,19 @@ int zeta_engine_search(const uint64_t board[7], int stm, int depth, int ply_init
  * and the PV (n x 64, may be NULL). */
 int zeta_engine_batch(const uint64_t *boards, const uint8_t *stm, int n, int depth, int workers, uint64_t max_nodes,
                       int32_t *scores, uint32_t *bestmoves, uint64_t *nodes, uint32_t *pvs);
+/* Iterative deepening 1..depth of n positions (rootsearch,
+ * src/search.c:35-223, batched): tables, killer and counter moves start
+ * empty and carry over between depths; a position stops deepening on a
+ * mate it cannot improve, when it has no move, or when worker 0 exceeded
+ * max_nodes in one depth (0 = no budget).  ordering: 0 the reference's
+ * move ordering, 1 / 2 the move-ordering network (BF16 / FP8) orders the
+ * quiet moves at nodes with >= 3 plies left.  Outputs per position: score
+ * and best move of the deepest finished depth, nodes summed over depths
+ * and workers, that depth (may be NULL); times in ms (wall, search
+ * kernels, network; may be NULL). */
+int zeta_engine_id(const uint64_t *boards, const uint8_t *stm, int n, int depth, int workers, uint64_t max_nodes,
+                   int ordering, int32_t *scores, uint32_t *bestmoves, uint64_t *nodes, uint8_t *depth_done,
+                   float *ms_total, float *ms_search, float *ms_net);
 
 /* ------------------------------------------------------------------ */
 /* The move-ordering network (no counterpart in the reference): 768

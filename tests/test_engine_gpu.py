@@ -127,3 +127,36 @@ def test_engine_node_budget_stops_the_search(zeta_device):
     z.tt_clear()
     pv, cnt = z.engine_search(b, stm, 12, 1, max_nodes=5000)
     assert cnt[0, 1] == 5001 and not pv.any()  # stopped: no PV, as the reference leaves it
+
+
+def test_engine_iterative_deepening_matches_reference(zeta_device):
+    """zeta_engine_id over 4 positions equals, per position, the reference's
+    iterative deepening with tables of a quarter of the size."""
+    _need_reference()
+    z = zeta_device
+    w = z.WORKLOADS["engine"]
+    boards, stm, _ = ol.make_positions(w["seed"] + 3, 4, min_plies=w["min_plies"], max_plies=w["max_plies"],
+                                       min_pieces=w["min_pieces"], min_depth=0, max_depth=0)
+    sc, mv, nodes, dd, *_ = z.engine_id(boards, stm, 6, 1)
+    for i in range(4):
+        ref = ol.RefSearch(E1 // 4, E2 // 4)
+        total = 0
+        for d in range(1, 7):
+            pv_r, c_r = ref.run(boards[i], int(stm[i]), d)
+            total += int(c_r[0, 1])
+        assert dd[i] == 6 and sc[i] == np.int32(pv_r[0]) and mv[i] == pv_r[1] and nodes[i] == total, i
+
+
+def test_engine_learned_ordering_runs(zeta_device):
+    """The network orders quiet moves: the search still returns legal best
+    moves, and the network's time is accounted."""
+    z = zeta_device
+    z.mlp_init(3)
+    w = z.WORKLOADS["engine"]
+    boards, stm, _ = ol.make_positions(w["seed"] + 4, 16, min_plies=w["min_plies"], max_plies=w["max_plies"],
+                                       min_pieces=w["min_pieces"], min_depth=0, max_depth=0)
+    for ordering in (1, 2):
+        sc, mv, nodes, dd, ms, ms_s, ms_n = z.engine_id(boards, stm, 6, 4, ordering)
+        assert (dd >= 1).all() and ms_n > 0
+        for i in range(16):
+            assert int(mv[i]) in ol.genmoves(boards[i], int(stm[i]))

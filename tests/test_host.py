@@ -78,6 +78,27 @@ def test_zeta_selftest_passes_all_14():
 
 
 @pytest.mark.gpu
+def test_zeta_go_prints_the_reference_search():
+    """`go` through the six cl_* calls: every iterative-deepening line
+    (depth, score, cumulative nodes, PV) equals the reference kernel's own
+    search with the host's default tables (256 MB TT1, no TT2)."""
+    if ol.reference() is None:
+        pytest.skip("reference kernels (oracle/_ref) not built")
+    r = subprocess.run([ZETA], input="new\nsd 6\ngo\nquit\n", capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert r.returncode == 0, r.stderr
+    lines = [l.split() for l in r.stdout.splitlines() if l[:1].isdigit()]
+    assert [int(f[0]) for f in lines] == [1, 2, 3, 4, 5, 6]
+    b, stm = ol.setboard("rnbqkbnr/pppppppp/8/8/8/8/PPPPPPPP/RNBQKBNR w KQkq - 0 1")
+    ref = ol.RefSearch(1 << 24, 0)
+    total = 0
+    for f in lines:
+        pv, cnt = ref.run(b, stm, int(f[0]))
+        total += int(cnt[0, 1])
+        assert int(f[1]) == int(np.int32(pv[0])) and int(f[3]) == total
+        assert f[4:] == [ol.move2can(int(m)) for m in pv[1:1 + int(f[0])] if m]
+
+
+@pytest.mark.gpu
 def test_zeta_xboard_session_plays_a_legal_move():
     session = "xboard\nprotover 2\nnew\nsd 4\nusermove e2e4\nquit\n"
     r = subprocess.run([ZETA], input=session, capture_output=True, text=True, timeout=600, cwd=ROOT)

@@ -88,6 +88,9 @@ SIGNATURES = {
                                           ctypes.c_int, _u32p, _u64p]),
     "zeta_engine_batch": (ctypes.c_int, [_u64p, _u8p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_uint64,
                                          _i32p, _u32p, _u64p, _u32p]),
+    "zeta_engine_id": (ctypes.c_int, [_u64p, _u8p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_uint64,
+                                      ctypes.c_int, _i32p, _u32p, _u64p, _u8p, ctypes.POINTER(ctypes.c_float),
+                                      ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]),
     "zeta_search_batch_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
                                                 ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                                 ctypes.c_void_p]),
@@ -353,6 +356,23 @@ def engine_batch(boards, stm, depth: int, workers: int = 1, max_nodes: int = (1 
                                             _ptr(scores, _i32p), _ptr(moves, _u32p), _ptr(nodes, _u64p),
                                             _ptr(pvs, _u32p) if with_pv else None))
     return (scores, moves, nodes, pvs) if with_pv else (scores, moves, nodes)
+
+
+def engine_id(boards, stm, depth: int, workers: int = 1, ordering: int = 0, max_nodes: int = 0):
+    """Iterative deepening of n positions with the full engine: (scores,
+    best moves, nodes, depth reached, ms_total, ms_search, ms_network)."""
+    b = np.ascontiguousarray(boards, dtype=np.uint64).reshape(-1, 7)
+    s = np.ascontiguousarray(stm, dtype=np.uint8)
+    n = b.shape[0]
+    scores = np.zeros(n, dtype=np.int32)
+    moves = np.zeros(n, dtype=np.uint32)
+    nodes = np.zeros(n, dtype=np.uint64)
+    dd = np.zeros(n, dtype=np.uint8)
+    t = [ctypes.c_float() for _ in range(3)]
+    _check(load_library().zeta_engine_id(_ptr(b, _u64p), _ptr(s, _u8p), n, depth, workers, max_nodes, ordering,
+                                         _ptr(scores, _i32p), _ptr(moves, _u32p), _ptr(nodes, _u64p), _ptr(dd, _u8p),
+                                         ctypes.byref(t[0]), ctypes.byref(t[1]), ctypes.byref(t[2])))
+    return scores, moves, nodes, dd, t[0].value, t[1].value, t[2].value
 
 
 def search_set_learned_order(top: int = 12, quiet_only: bool = True) -> None:

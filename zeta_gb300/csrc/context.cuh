@@ -148,6 +148,7 @@ int search_id(const uint64_t *boards, const uint8_t *stm, int n, int depth, int 
 int mlp_fill_order_cache(const OrderRequest *req, uint32_t nreq, OrderEntry *cache, uint64_t mask, int fp8,
                          cudaStream_t s);
 bool mlp_ready_for_search();
+int learn_buffers();
 int search_tt_clear(cudaStream_t s);
 /* mlp.cu */
 void mlp_free();

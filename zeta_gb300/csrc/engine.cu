@@ -143,7 +143,8 @@ void engine_free() {
 /* One fixed-depth launch over n positions already staged in g_eng
  * (boards, stm, ply, active, optional history).  Each position gets a
  * power-of-two slice of TT1 / TT2. */
-int engine_launch(int n, int w, int depth, uint64_t max_nodes, bool with_hist, bool with_active, float *kernel_ms) {
+int engine_launch(int n, int w, int depth, uint64_t max_nodes, bool with_hist, bool with_active, float *kernel_ms,
+                  bool learned = false) {
   Context &c = ctx();
   EngineState &e = g_eng;
   if (c.tt_owner != 2) {
@@ -177,6 +178,14 @@ int engine_launch(int n, int w, int depth, uint64_t max_nodes, bool with_hist, b
   a.finito = e.finito;
   a.pv = e.pv;
   a.status = e.status;
+  if (learned) {
+    a.ocache = (OrderEntry *)c.s_ocache;
+    a.ocache_mask = c.s_ocache_entries - 1;
+    a.oreq = (OrderRequest *)c.s_oreq;
+    a.noreq = c.s_noreq;
+    a.oreq_cap = c.s_oreq_cap;
+    a.learned_top = c.s_learned_top;
+  }
   ZCHECK(cudaMemsetAsync(e.finito, 0, n * sizeof(uint32_t), c.stream));
   ZCHECK(cudaMemsetAsync(e.pv, 0, (size_t)n * kEPly * sizeof(uint32_t), c.stream));
   ZCHECK(cudaMemsetAsync(e.status, 0, sizeof(uint32_t), c.stream));
@@ -277,5 +286,103 @@ extern "C" int zeta_engine_batch(const uint64_t *boards, const uint8_t *stm, int
     nodes[i] = s;
   }
   if (pvs) memcpy(pvs, pv.data(), pv.size() * sizeof(uint32_t));
+  return ZETA_OK;
+}
+
+/* Iterative deepening 1..depth over a batch (rootsearch,
+ * src/search.c:35-223, for n positions at once): tables, killer and
+ * counter moves start empty and carry over between depths; a position
+ * stops deepening on a mate-in-n it cannot improve, on a missing move or
+ * when worker 0 ran out of its node budget.  ordering 1 / 2: the
+ * move-ordering network (BF16 / FP8) orders the quiet moves of nodes with
+ * >= 3 plies left, from requests logged in the previous depth. */
+extern "C" int zeta_engine_id(const uint64_t *boards, const uint8_t *stm, int n, int depth, int workers,
+                              uint64_t max_nodes, int ordering, int32_t *scores, uint32_t *bestmoves, uint64_t *nodes,
+                              uint8_t *depth_done, float *ms_total, float *ms_search, float *ms_net) {
+  Context &c = ctx();
+  if (!c.ready) return set_error(ZETA_ERR_STATE, "zeta_init has not been called");
+  if (!boards || !stm || !scores || !bestmoves || !nodes) return set_error(ZETA_ERR_ARG, "null pointer");
+  if (n < 1 || depth < 1 || depth >= kEPly || workers < 1 || (long long)n * workers > (1ll << 24) || ordering < 0 ||
+      ordering > 2)
+    return set_error(ZETA_ERR_ARG, "engine id: n %d depth %d workers %d ordering %d out of range", n, depth, workers,
+                     ordering);
+  const bool learned = ordering > 0;
+  if (learned && !mlp_ready_for_search())
+    return set_error(ZETA_ERR_STATE, "learned ordering needs zeta_mlp_init (and training or parameters)");
+  int rc = engine_stage(boards, stm, n, workers, nullptr, nullptr, 0);
+  if (rc) return rc;
+  rc = engine_clear(c.stream);
+  if (rc) return rc;
+  c.tt_owner = 2;
+  if (learned) {
+    rc = learn_buffers();
+    if (rc) return rc;
+    ZCHECK(cudaMemsetAsync(c.s_ocache, 0, c.s_ocache_entries * sizeof(OrderEntry), c.stream));
+    ZCHECK(cudaMemsetAsync(c.s_noreq, 0, 4, c.stream));
+  }
+  EngineState &e = engine_state();
+  std::vector<uint8_t> active(n, 1);
+  std::vector<uint32_t> pv((size_t)n * kEPly);
+  std::vector<unsigned long long> cnt((size_t)n * workers * 4);
+  for (int i = 0; i < n; i++) {
+    scores[i] = 0;
+    bestmoves[i] = 0;
+    nodes[i] = 0;
+    if (depth_done) depth_done[i] = 0;
+  }
+  float t_search = 0.f, t_net = 0.f;
+  const uint64_t budget = max_nodes ? max_nodes : ~0ULL;
+  ZCHECK(cudaEventRecord(c.ev[2], c.stream));
+  for (int d = 1; d <= depth; d++) {
+    int live = 0;
+    for (int i = 0; i < n; i++) live += active[i];
+    if (!live) break;
+    ZCHECK(cudaMemcpyAsync(e.active, active.data(), n, cudaMemcpyHostToDevice, c.stream));
+    float ms = 0.f;
+    rc = engine_launch(n, workers, d, budget, false, true, &ms, learned);
+    if (rc) return rc;
+    t_search += ms;
+    ZCHECK(cudaMemcpy(pv.data(), e.pv, pv.size() * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    ZCHECK(cudaMemcpy(cnt.data(), e.cnt, cnt.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+    for (int i = 0; i < n; i++) {
+      if (!active[i]) continue;
+      for (int w = 0; w < workers; w++) nodes[i] += cnt[((size_t)w * n + i) * 4];
+      const uint32_t *P = &pv[(size_t)i * kEPly];
+      const bool stopped = cnt[(size_t)i * 4] >= budget;
+      if (stopped || (P[1] & 0x3FFFFFFFu) == 0) {
+        active[i] = 0;
+        continue;
+      }
+      const int sc = (int32_t)P[0];
+      bestmoves[i] = P[1];
+      scores[i] = is_inf(sc) ? 0 : sc;
+      if (depth_done) depth_done[i] = (uint8_t)d;
+      if ((sc >= E_MATE && sc < E_INF && d >= E_INF - sc) || (sc <= -E_MATE && sc > -E_INF && d >= E_INF + sc))
+        active[i] = 0; /* mate in n found */
+    }
+    if (learned && d < depth) {
+      uint32_t nreq = 0;
+      ZCHECK(cudaMemcpy(&nreq, c.s_noreq, 4, cudaMemcpyDeviceToHost));
+      if (nreq > c.s_oreq_cap) nreq = c.s_oreq_cap;
+      ZCHECK(cudaEventRecord(c.ev[0], c.stream));
+      if (nreq)
+        rc = mlp_fill_order_cache((const OrderRequest *)c.s_oreq, nreq, (OrderEntry *)c.s_ocache,
+                                  c.s_ocache_entries - 1, ordering == 2, c.stream);
+      if (rc) return rc;
+      ZCHECK(cudaEventRecord(c.ev[1], c.stream));
+      ZCHECK(cudaEventSynchronize(c.ev[1]));
+      float mm = 0.f;
+      ZCHECK(cudaEventElapsedTime(&mm, c.ev[0], c.ev[1]));
+      t_net += mm;
+      ZCHECK(cudaMemsetAsync(c.s_noreq, 0, 4, c.stream));
+    }
+  }
+  ZCHECK(cudaEventRecord(c.ev[3], c.stream));
+  ZCHECK(cudaEventSynchronize(c.ev[3]));
+  float tot = 0.f;
+  ZCHECK(cudaEventElapsedTime(&tot, c.ev[2], c.ev[3]));
+  if (ms_total) *ms_total = tot;
+  if (ms_search) *ms_search = t_search;
+  if (ms_net) *ms_net = t_net;
   return ZETA_OK;
 }

@@ -101,6 +101,7 @@ struct EFrame {
   int alpha, beta, depth, todo, mc;
   Move mh, iid; /* localMoveHistory, localIIDMoves */
   uint8_t state, mode, hmc, mi; /* node state, search mode, half-move clock, list index of mh */
+  uint16_t lmv[kOrderTop];      /* the network's best (from | to << 6) moves, 0xFFFF = none */
 };
 
 struct EngineArgs {
@@ -125,6 +126,13 @@ struct EngineArgs {
   uint32_t *finito;    /* N: gid+1 of the first worker back at the root */
   uint32_t *pv;        /* N x 64: PV[0] score, PV[1..] moves */
   uint32_t *status;
+  /* learned ordering (no reference counterpart): null cache = off */
+  OrderEntry *ocache;
+  u64 ocache_mask;
+  OrderRequest *oreq;
+  uint32_t *noreq;
+  uint32_t oreq_cap;
+  int learned_top;
 };
 
 /* the move-ordering score of the reference's picker (zeta.cl:2087-2124) */
@@ -232,7 +240,8 @@ namespace {
  * Returns the list index or -1.  Counts TT-move and IID-move sightings as
  * the reference's COUNTERS[3] / [5] do. */
 __host__ __device__ int pick_move(const Move *L, const u64 *mask, int stm, Move killer, Move counter, Move iid, Move ttm,
-                         bool randomize, uint32_t &prn, const EvalTables &T, unsigned long long *C) {
+                         bool randomize, uint32_t &prn, const EvalTables &T, unsigned long long *C,
+                         const uint16_t *lmv, int ltop) {
   int best = -1, bs = 0, bf = 0, bt = 0;
   for (int wd = 0; wd < 4; wd++) {
     u64 b = mask[wd];
@@ -241,6 +250,15 @@ __host__ __device__ int pick_move(const Move *L, const u64 *mask, int stm, Move 
       b &= b - 1;
       const Move m = L[i];
       int s = pick_score(m, stm, T);
+      if (lmv && (m_pcpt(m) >> 1) == PNONE) {
+        /* learned: the network's quiet moves after the counter move */
+        const uint16_t k = (uint16_t)(m_from(m) | (m_to(m) << 6));
+        for (int r = 0; r < ltop; r++)
+          if (lmv[r] == k) {
+            s = T.value[QUEEN] + T.value[PAWN] - 1 - r;
+            break;
+          }
+      }
       if (m == counter) s = T.value[QUEEN] + T.value[PAWN];
       if (m == killer) s = T.value[QUEEN] + 2 * T.value[PAWN];
       if (randomize) {
@@ -439,6 +457,41 @@ __host__ __device__ void engine_worker(const EngineArgs &a, long long t, const E
         }
       }
       f->mc = movecount;
+      if (a.ocache) {
+        /* the network's ordering of this node: from the cache at >= 3 plies
+         * left, else requested for the next iteration from >= 2 plies */
+        for (int r = 0; r < kOrderTop; r++) f->lmv[r] = 0xFFFF;
+        if (movecount > 1 && !qs && f->depth >= 2) {
+          OrderEntry *oe = a.ocache + (f->hash & a.ocache_mask);
+          const unsigned long long ek = ((volatile unsigned long long *)&oe->key)[0];
+          if (ek == f->hash) {
+            if (f->depth >= 3)
+              for (int r = 0; r < kOrderTop; r++) f->lmv[r] = oe->mv[r];
+          } else {
+#if defined(__CUDA_ARCH__)
+            const uint32_t idx = atomicAdd(a.noreq, 1u);
+#else
+            const uint32_t idx = (*a.noreq)++;
+#endif
+            if (idx < a.oreq_cap) {
+              OrderRequest q;
+              q.key = f->hash;
+              q.b[0] = pos.b0;
+              q.b[1] = pos.p1;
+              q.b[2] = pos.p2;
+              q.b[3] = pos.p3;
+              q.b[4] = pos.cr;
+              q.stm = stm;
+              q.pad = 0;
+              a.oreq[idx] = q;
+              OrderEntry pend; /* requested: other workers do not ask again */
+              pend.key = f->hash;
+              for (int r = 0; r < kOrderTop; r++) pend.mv[r] = 0xFFFF;
+              *oe = pend;
+            }
+          }
+        }
+      }
       for (int j = 0; j < 4; j++) {
         const int lo = j * 64;
         f->m1[j] = ngen <= lo ? 0ULL : (ngen >= lo + 64 ? ~0ULL : ((1ULL << (ngen - lo)) - 1));
@@ -557,7 +610,8 @@ __host__ __device__ void engine_worker(const EngineArgs &a, long long t, const E
     const Move *L = MV + sd * kEMoves;
     int pick = -1;
     if (lmove == 0 && !bresearch) {
-      pick = pick_move(L, g->m1, stm, killer, counter, g->iid, ttmove, brandomize, prn, sT, C);
+      pick = pick_move(L, g->m1, stm, killer, counter, g->iid, ttmove, brandomize, prn, sT, C,
+                       a.ocache ? g->lmv : nullptr, a.learned_top);
       if (pick >= 0) lmove = L[pick];
     }
     if (lmove == 0 && (g->state & ST_ITER1)) {
@@ -565,7 +619,8 @@ __host__ __device__ void engine_worker(const EngineArgs &a, long long t, const E
       g->state |= ST_ITER2;
     }
     if (lmove == 0 && !bresearch) {
-      pick = pick_move(L, g->m2, stm, killer, counter, g->iid, ttmove, brandomize, prn, sT, C);
+      pick = pick_move(L, g->m2, stm, killer, counter, g->iid, ttmove, brandomize, prn, sT, C,
+                       a.ocache ? g->lmv : nullptr, a.learned_top);
       if (pick >= 0) lmove = L[pick];
     }
 

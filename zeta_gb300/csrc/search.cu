@@ -508,7 +508,7 @@ int search_tt_clear(cudaStream_t s) {
 }
 
 /* ordering cache and request log of the learned ordering */
-static int learn_buffers() {
+int learn_buffers() {
   Context &c = ctx();
   if (!c.s_ocache) {
     c.s_ocache_entries = 1ull << 22; /* 128 MiB of 32-byte entries */

@@ -23,6 +23,7 @@ enum { PNONE = 0, PAWN = 1, KNIGHT = 2, KING = 3, BISHOP = 4, ROOK = 5, QUEEN = 
 #define MAXGAMEPLY 1024
 #define INF 32000
 #define MATESCORE 30000
+#define ESTEBF 3 /* estimated effective branching factor (src/types.h:81) */
 #define MOVENONE 0u
 #define NULLMOVE 0x41u
 

@@ -55,8 +55,17 @@ bool cl_run_perft(bool stm, int32_t depth) {
 
 bool cl_run_alphabeta(bool stm, int32_t depth, uint64_t nodes) {
   if (!g_inited) return false;
-  if (zeta_search(GLOBAL_BOARD, stm ? 1 : 0, depth, PLY, GLOBAL_HASHHISTORY, nodes, PV, COUNTERS) != ZETA_OK)
-    return fail("zeta_search");
+  if (search_mode == 0) {
+    /* pure fixed-depth search (no reference counterpart): root = negamax */
+    memset(COUNTERS, 0, totalWorkUnits * 64 * sizeof(uint64_t));
+    if (zeta_search(GLOBAL_BOARD, stm ? 1 : 0, depth, PLY, GLOBAL_HASHHISTORY, nodes, PV, COUNTERS) != ZETA_OK)
+      return fail("zeta_search");
+    return true;
+  }
+  /* the reference's search: totalWorkUnits workers, COUNTERS per worker */
+  if (zeta_engine_search(GLOBAL_BOARD, stm ? 1 : 0, depth, PLY, GLOBAL_HASHHISTORY, nodes, (int)totalWorkUnits, PV,
+                         COUNTERS) != ZETA_OK)
+    return fail("zeta_engine_search");
   return true;
 }
 

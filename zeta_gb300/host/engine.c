@@ -26,7 +26,7 @@ uint64_t tt1_memory = 256, tt2_memory = 0;
 int64_t nodes_per_second = 1000000;
 uint64_t MaxNodes = 0;
 int device_id = 0;
-int search_mode = 0;
+int search_mode = 1;
 uint64_t ABNODECOUNT = 0, TTHITS = 0, TTSCOREHITS = 0, IIDHITS = 0;
 FILE *LogFile = NULL;
 
@@ -142,27 +142,44 @@ Move rootsearch(Bitboard *board, int stm, int depth) {
     memcpy(&GLOBAL_HASHHISTORY[i * MAXGAMEPLY], HashHistory, sizeof HashHistory);
     for (int j = 0; j < 64; j++) RNUMBERS[i * 64 + j] = (uint32_t)rand();
   }
-  for (int idf = 1; idf <= depth && idf < MAXPLY; idf++) {
+  /* node budget of a move (the reference derives it from the clock,
+   * src/xboard.c:193); 0 = no budget, for depth-limited searches */
+  const uint64_t max_nodes = MaxNodes ? MaxNodes : UINT64_MAX / ESTEBF;
+  const uint64_t budget = max_nodes / totalWorkUnits;
+  int idf = 1;
+  do {
     memset(COUNTERS, 0, totalWorkUnits * 64 * sizeof(uint64_t));
-    if (!cl_write_objects() || !cl_run_alphabeta(stm, idf, MaxNodes / totalWorkUnits) || !cl_read_memory()) die();
+    if (!cl_write_objects() || !cl_run_alphabeta(stm, idf, budget) || !cl_read_memory()) die();
     for (uint64_t i = 0; i < totalWorkUnits; i++) {
       ABNODECOUNT += COUNTERS[i * 64 + 1];
       TTHITS += COUNTERS[i * 64 + 3];
       TTSCOREHITS += COUNTERS[i * 64 + 4];
       IIDHITS += COUNTERS[i * 64 + 5];
     }
-    if (JUSTMOVE(PV[1]) == MOVENONE) break; /* no legal move */
-    best = PV[1];
-    score = (int32_t)PV[0];
     double el = (get_time_ms() - start) / 1000.0;
-    /* xboard mate scores, src/search.c:131-137 */
-    int xs = score <= -MATESCORE ? -100000 - (INF + score) : score >= MATESCORE ? 100000 - (-INF + score) : score;
-    char mv[6];
-    move2can(best, mv);
-    printf("%d %d %d %" PRIu64 " %s\n", idf, xs, (int)(el * 100), ABNODECOUNT, mv);
-    if (LogFile) fprintf(LogFile, "%d %d %d %" PRIu64 " %s\n", idf, xs, (int)(el * 100), ABNODECOUNT, mv);
-    fflush(stdout);
-    if (score >= MATESCORE || score <= -MATESCORE) break; /* mate found */
-  }
+    if (idf == 1 && JUSTMOVE(PV[1]) != MOVENONE) best = PV[1]; /* a move anyway */
+    if (COUNTERS[1] < budget) { /* not stopped by the node budget */
+      if (JUSTMOVE(PV[1]) != MOVENONE) best = PV[1];
+      score = ((int32_t)PV[0] == INF || (int32_t)PV[0] == -INF) ? 0 : (int32_t)PV[0];
+      /* xboard mate scores, src/search.c:131-137 */
+      int xs = score <= -MATESCORE ? -100000 - (INF + score) : score >= MATESCORE ? 100000 - (-INF + score) : score;
+      if (JUSTMOVE(PV[1]) == MOVENONE) break;
+      printf("%d %d %d %" PRIu64, idf, xs, (int)(el * 100), ABNODECOUNT);
+      if (LogFile) fprintf(LogFile, "%d %d %d %" PRIu64, idf, xs, (int)(el * 100), ABNODECOUNT);
+      for (int i = 1; i < MAXPLY && i <= idf && JUSTMOVE(PV[i]) != MOVENONE; i++) {
+        char mv[6];
+        move2can(PV[i], mv);
+        printf(" %s", mv);
+        if (LogFile) fprintf(LogFile, " %s", mv);
+      }
+      printf("\n");
+      if (LogFile) fprintf(LogFile, "\n");
+      fflush(stdout);
+    }
+    /* mate in n: no deeper iteration can change it (src/search.c:180-191) */
+    if (score >= MATESCORE && score < INF && idf >= INF - score) break;
+    if (score <= -MATESCORE && score > -INF && idf >= INF + score) break;
+    idf++;
+  } while (idf <= depth && ABNODECOUNT * ESTEBF <= max_nodes && ABNODECOUNT > 1 && idf < MAXPLY);
   return best;
 }

@@ -34,7 +34,7 @@ extern uint64_t tt1_memory, tt2_memory;
 extern int64_t nodes_per_second;
 extern uint64_t MaxNodes;
 extern int device_id;
-extern int search_mode;          /* 0 pure fixed-depth, 1 full engine */
+extern int search_mode;          /* 1 the reference's search (default), 0 pure fixed-depth */
 
 /* results */
 extern uint64_t ABNODECOUNT, TTHITS, TTSCOREHITS, IIDHITS;

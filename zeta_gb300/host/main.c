@@ -2,7 +2,7 @@
  * main.c -- the zeta host binary (src/zeta.c:525-709): options, config,
  * device start-up, then the xboard command loop.
  *
- *   zeta [-s|--selftest] [-l|--log] [-d <device>] [-c <config.txt>] [-v] [-h]
+ *   zeta [-s|--selftest] [-l|--log] [-p|--pure] [-d <device>] [-c <config.txt>] [-v] [-h]
  */
 #include <stdlib.h>
 #include <string.h>
@@ -14,6 +14,8 @@ static void usage(void) {
   printf("Zeta GB300 -- the Zeta chess engine's device path on Blackwell GPUs.\n"
          "  -s, --selftest   run the 14 perft known-answer tests and exit\n"
          "  -l, --log        append a log to zeta.log\n"
+         "  -p, --pure       pure fixed-depth alpha-beta (root score = negamax) instead of\n"
+         "                   the reference's search with its heuristics\n"
          "  -d <n>           CUDA device (default 0)\n"
          "  -c <file>        config file (default config.txt: threadsX, threadsY, tt1_memory, ...)\n"
          "  -v, --version    print the version\n"
@@ -35,6 +37,8 @@ int main(int argc, char **argv) {
       return 0;
     } else if (!strcmp(argv[i], "-s") || !strcmp(argv[i], "--selftest")) {
       run_selftest = true;
+    } else if (!strcmp(argv[i], "-p") || !strcmp(argv[i], "--pure")) {
+      search_mode = 0;
     } else if (!strcmp(argv[i], "-l") || !strcmp(argv[i], "--log")) {
       LogFile = fopen("zeta.log", "a");
     } else if (!strcmp(argv[i], "-d") && i + 1 < argc) {
