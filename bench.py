@@ -51,6 +51,25 @@ def _opcounts():
     return None, None
 
 
+def _node_roofline(z, nodes_per_s: float, key: str, kernel: str):
+    """int32-ALU roofline of a search kernel: nodes/s x algorithmic ops per
+    node (profiles/opcount.json) against the measured integer peak."""
+    path = os.path.join(ROOT, "profiles", "opcount.json")
+    if not os.path.exists(path):
+        return None
+    ops = json.load(open(path)).get(key)
+    try:
+        peak = z.int_peak_tops()
+    except Exception:  # noqa: BLE001 -- the microbenchmark is optional
+        return None
+    if not ops or not peak:
+        return None
+    achieved = nodes_per_s * ops / 1e12
+    return {"bound": "int32-alu", "achieved": round(achieved, 4), "peak": round(peak, 3), "unit": "Tops/s",
+            "frac": round(achieved / peak, 4), "traffic": None, "ops_per_node": ops, "kernel": kernel,
+            "peak_source": "measured: int32 LOP3/SHF/IADD3 microbenchmark (zeta_int_peak)"}
+
+
 def dist_env():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -360,6 +379,7 @@ def run_search(args):
                        "tt": "1 GiB, 16-byte entries, cleared every step"},
             "nodes_per_s": round(r["nodes_per_s"], 1), "nodes_per_step": r["nodes_per_step"],
             "sweep": {str(k): round(v["positions_per_s"], 2) for k, v in results.items()},
+            "roofline": _node_roofline(z, r["nodes_per_s"], "ops_per_search_node", "k_search_pure"),
         }), flush=True)
     z.release()
 
@@ -404,6 +424,7 @@ def run_engine(args):
                    "workers_per_position": workers, "tt": "8 GB TT1 + 2 GB TT2, 1/n per position"},
         "nodes_per_s": round(p["nodes"] / (p["ms_total"] / 1e3), 1), "nodes": p["nodes"],
         "clocks": clocks.summary(),
+        "roofline": _node_roofline(z, p["nodes"] / (p["ms_total"] / 1e3), "ops_per_engine_node", "k_engine"),
     }
     if 1 in res:
         l1 = res[1]

@@ -101,7 +101,8 @@ struct EFrame {
   int alpha, beta, depth, todo, mc;
   Move mh, iid; /* localMoveHistory, localIIDMoves */
   uint8_t state, mode, hmc, mi; /* node state, search mode, half-move clock, list index of mh */
-  uint16_t lmv[kOrderTop];      /* the network's best (from | to << 6) moves, 0xFFFF = none */
+  u64 lmask[4];                 /* list indices of the network's best moves */
+  uint8_t lidx[kOrderTop];      /* their list indices, best first (0xFF = none) */
 };
 
 struct EngineArgs {
@@ -241,7 +242,7 @@ namespace {
  * the reference's COUNTERS[3] / [5] do. */
 __host__ __device__ int pick_move(const Move *L, const u64 *mask, int stm, Move killer, Move counter, Move iid, Move ttm,
                          bool randomize, uint32_t &prn, const EvalTables &T, unsigned long long *C,
-                         const uint16_t *lmv, int ltop) {
+                         const EFrame *lf, int ltop) {
   int best = -1, bs = 0, bf = 0, bt = 0;
   for (int wd = 0; wd < 4; wd++) {
     u64 b = mask[wd];
@@ -250,11 +251,10 @@ __host__ __device__ int pick_move(const Move *L, const u64 *mask, int stm, Move 
       b &= b - 1;
       const Move m = L[i];
       int s = pick_score(m, stm, T);
-      if (lmv && (m_pcpt(m) >> 1) == PNONE) {
-        /* learned: the network's quiet moves after the counter move */
-        const uint16_t k = (uint16_t)(m_from(m) | (m_to(m) << 6));
+      if (lf && ((lf->lmask[i >> 6] >> (i & 63)) & 1) && (m_pcpt(m) >> 1) == PNONE) {
+        /* learned: the network's quiet moves right after the counter move */
         for (int r = 0; r < ltop; r++)
-          if (lmv[r] == k) {
+          if (lf->lidx[r] == i) {
             s = T.value[QUEEN] + T.value[PAWN] - 1 - r;
             break;
           }
@@ -460,13 +460,23 @@ __host__ __device__ void engine_worker(const EngineArgs &a, long long t, const E
       if (a.ocache) {
         /* the network's ordering of this node: from the cache at >= 3 plies
          * left, else requested for the next iteration from >= 2 plies */
-        for (int r = 0; r < kOrderTop; r++) f->lmv[r] = 0xFFFF;
+        for (int j = 0; j < 4; j++) f->lmask[j] = 0;
+        for (int r = 0; r < kOrderTop; r++) f->lidx[r] = 0xFF;
         if (movecount > 1 && !qs && f->depth >= 2) {
           OrderEntry *oe = a.ocache + (f->hash & a.ocache_mask);
           const unsigned long long ek = ((volatile unsigned long long *)&oe->key)[0];
           if (ek == f->hash) {
             if (f->depth >= 3)
-              for (int r = 0; r < kOrderTop; r++) f->lmv[r] = oe->mv[r];
+              for (int r = 0; r < a.learned_top && r < kOrderTop; r++) {
+                const uint16_t k = oe->mv[r];
+                if (k == 0xFFFF) break;
+                for (int j = 0; j < ngen; j++)
+                  if ((uint16_t)(m_from(L[j]) | (m_to(L[j]) << 6)) == k) {
+                    f->lidx[r] = (uint8_t)j;
+                    f->lmask[j >> 6] |= 1ULL << (j & 63);
+                    break;
+                  }
+              }
           } else {
 #if defined(__CUDA_ARCH__)
             const uint32_t idx = atomicAdd(a.noreq, 1u);
@@ -611,7 +621,7 @@ __host__ __device__ void engine_worker(const EngineArgs &a, long long t, const E
     int pick = -1;
     if (lmove == 0 && !bresearch) {
       pick = pick_move(L, g->m1, stm, killer, counter, g->iid, ttmove, brandomize, prn, sT, C,
-                       a.ocache ? g->lmv : nullptr, a.learned_top);
+                       a.ocache ? g : nullptr, a.learned_top);
       if (pick >= 0) lmove = L[pick];
     }
     if (lmove == 0 && (g->state & ST_ITER1)) {
@@ -620,7 +630,7 @@ __host__ __device__ void engine_worker(const EngineArgs &a, long long t, const E
     }
     if (lmove == 0 && !bresearch) {
       pick = pick_move(L, g->m2, stm, killer, counter, g->iid, ttmove, brandomize, prn, sT, C,
-                       a.ocache ? g->lmv : nullptr, a.learned_top);
+                       a.ocache ? g : nullptr, a.learned_top);
       if (pick >= 0) lmove = L[pick];
     }
 
