@@ -471,11 +471,15 @@ def run_gemm(args):
         A8, B8 = A.to(torch.float8_e4m3fn), B.to(torch.float8_e4m3fn)
         flops = 2.0 * M * N * K
         res = {"M": M, "N": N, "K": K}
-        for name, fn in (("bf16", lambda: z.gemm_tc(A.data_ptr(), B.data_ptr(), C.data_ptr(), M, N, K, False,
-                                                     stream.cuda_stream)),
-                         ("fp8", lambda: z.gemm_tc(A8.data_ptr(), B8.data_ptr(), C.data_ptr(), M, N, K, True,
-                                                    stream.cuda_stream)),
-                         ("cublas_bf16", lambda: torch.matmul(A, B.t()))):
+        cases = []
+        for c in (1, 2):  # shared-memory ring sized for 1 or 2 resident CTAs per SM
+            cases += [(f"bf16_c{c}", c, lambda: z.gemm_tc(A.data_ptr(), B.data_ptr(), C.data_ptr(), M, N, K, False,
+                                                           stream.cuda_stream)),
+                      (f"fp8_c{c}", c, lambda: z.gemm_tc(A8.data_ptr(), B8.data_ptr(), C.data_ptr(), M, N, K, True,
+                                                          stream.cuda_stream))]
+        cases.append(("cublas_bf16", 1, lambda: torch.matmul(A, B.t())))
+        for name, ctas, fn in cases:
+            z.gemm_configure(ctas)
             for _ in range(args.warmup):
                 fn()
             ms = []
@@ -489,6 +493,10 @@ def run_gemm(args):
                 ms.append(e0.elapsed_time(e1))
             t = statistics.median(ms)
             res[name] = {"ms": round(t, 4), "tflops": round(flops / t / 1e9, 1)}
+        for kind in ("bf16", "fp8"):
+            best = min((1, 2), key=lambda c: res[f"{kind}_c{c}"]["ms"])
+            res[kind] = dict(res[f"{kind}_c{best}"], ctas_per_sm=best)
+        z.gemm_configure(res["bf16"]["ctas_per_sm"])
         ref = (A.float() @ B.float().t())
         z.gemm_tc(A.data_ptr(), B.data_ptr(), C.data_ptr(), M, N, K, False, stream.cuda_stream)
         res["bf16_max_rel_err"] = float(((C - ref).abs().max() / ref.abs().max()).item())

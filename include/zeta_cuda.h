@@ -232,6 +232,9 @@ int zeta_mlp_scores(const uint64_t *boards, const uint8_t *stm, int n, int fp8, 
  * (fp8 != 0), device buffers, K a multiple of 64 (BF16) or 128 (FP8), N a
  * multiple of 16.  tcgen05.mma with FP32 accumulation in tensor memory. */
 int zeta_gemm_tc(const void *d_A, const void *d_B, float *d_C, int M, int N, int K, int fp8, void *stream);
+/* Tuning knob of that kernel: the shared-memory ring is sized for 1
+ * (default, deepest pipeline) or 2 resident CTAs per SM. */
+int zeta_gemm_configure(int ctas_per_sm);
 
 /* ------------------------------------------------------------------ */
 /* Seeded synthetic positions generated on the device (the benchmark

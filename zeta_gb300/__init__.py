@@ -94,6 +94,7 @@ SIGNATURES = {
     "zeta_search_batch_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
                                                 ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                                 ctypes.c_void_p]),
+    "zeta_gemm_configure": (ctypes.c_int, [ctypes.c_int]),
     "zeta_gemm_tc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
                                     ctypes.c_int, ctypes.c_int, ctypes.c_void_p]),
     "zeta_mlp_init": (ctypes.c_int, [ctypes.c_uint64]),
@@ -238,6 +239,10 @@ def search_batch_device(d_boards: int, d_stm: int, n: int, depth: int, workers: 
 
 def search_set_helpers(max_workers_per_position: int) -> None:
     _check(load_library().zeta_search_set_helpers(max_workers_per_position))
+
+
+def gemm_configure(ctas_per_sm: int) -> None:
+    _check(load_library().zeta_gemm_configure(ctas_per_sm))
 
 
 def gemm_tc(d_a: int, d_b: int, d_c: int, m: int, n: int, k: int, fp8: bool = False, stream: int = 0) -> None:

@@ -21,6 +21,8 @@
  * Every wait is bounded; a timeout sets an error word and the kernel
  * still frees its tensor memory.
  */
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_bf16.h>
 #include <cuda_fp8.h>
 
@@ -54,117 +56,257 @@ struct GemmArgs {
   const unsigned *amaxA, *amaxB; /* FP8: per-tensor max |x| (float bits); scale *= amaxA*amaxB/448^2 */
 };
 
-/* BN: output columns per CTA (64, 128 or 256); FP8: operands are e4m3 */
+/* The product C[M x N] = A[M x K] . B[N x K]^T of one 128 x BN output
+ * tile (a K range of it when split-K), 128 threads:
+ *   thread 0   TMA producer: 128-byte-wide K slices of A and B into a ring
+ *              of `stages` shared-memory slots (128-byte swizzle, the
+ *              layout the MMA descriptors expect), one mbarrier per slot
+ *              counting the bytes in flight;
+ *   thread 32  MMA issuer: four tcgen05.mma per slot into the FP32
+ *              accumulator in tensor memory, then tcgen05.commit on the
+ *              slot's "empty" barrier so the producer can refill it, and
+ *              a final commit on `done`;
+ *   all warps  epilogue: warp w reads accumulator lanes 32w..32w+31 with
+ *              tcgen05.ld and applies scale, bias, ReLU, ReLU mask and the
+ *              FP32 / BF16 / transposed BF16 stores (atomic FP32 adds when
+ *              the K range is split across CTAs).
+ * Loads of slot s+stages overlap the MMAs of slot s.  Every wait is
+ * bounded: a timeout sets an error word, the producer's copies still in
+ * flight are awaited (bounded), tensor memory is freed. */
+constexpr int kMaxStages = 8;
+
 template <int BN, bool FP8>
-__global__ void __launch_bounds__(128) k_gemm(GemmArgs g) {
+__global__ void __launch_bounds__(128, 1)
+    k_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, GemmArgs g,
+           int kb_per_split, int stages) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t *base = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-  uint8_t *sA = base;           /* 128 rows x 128 bytes */
-  uint8_t *sB = base + 16384;   /* BN rows x 128 bytes */
-  __shared__ uint64_t bar;
+  constexpr uint32_t A_BYTES = 128 * 128, B_BYTES = BN * 128, STAGE = A_BYTES + B_BYTES;
+  __shared__ uint64_t full[kMaxStages], empty[kMaxStages], done;
   __shared__ uint32_t s_taddr;
+  __shared__ int s_fail, s_issued;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int m0 = blockIdx.x * 128, n0 = blockIdx.y * BN;
-  constexpr int EK = FP8 ? 128 : 64;           /* K elements per 128-byte row */
-  constexpr int ESZ = FP8 ? 1 : 2;             /* bytes per element */
+  constexpr int EK = FP8 ? 128 : 64; /* K elements per 128-byte row */
   constexpr uint32_t IDESC = FP8 ? tc::idesc_f8(128, BN) : tc::idesc_f16(128, BN, 1);
+  const int nkb = g.K / EK;
+  const int kb0 = blockIdx.z * kb_per_split;
+  const int cnt = min(nkb, kb0 + kb_per_split) - kb0;
 
   if (warp == 0) tc::tmem_alloc(&s_taddr, BN);
-  if (tid == 0) tc::mbar_init(&bar, 1);
+  if (tid == 0) {
+    for (int s = 0; s < stages; s++) {
+      tc::mbar_init(&full[s], 1);
+      tc::mbar_init(&empty[s], 1);
+    }
+    tc::mbar_init(&done, 1);
+    s_fail = 0;
+    s_issued = 0;
+    tc::prefetch_tmap(&tmA);
+    tc::prefetch_tmap(&tmB);
+  }
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t taddr = s_taddr;
-  const uint8_t *Ag = (const uint8_t *)g.A, *Bg = (const uint8_t *)g.B;
-  const size_t rowbytes = (size_t)g.K * ESZ;
-  uint32_t phase = 0;
-  int ok = 1;
-  for (int k0 = 0; k0 < g.K; k0 += EK) {
-    for (int i = tid; i < 128 * 8; i += 128) {
-      const int r = i >> 3, c = i & 7;
-      uint4 v = make_uint4(0, 0, 0, 0);
-      if (m0 + r < g.M) v = *(const uint4 *)(Ag + (size_t)(m0 + r) * rowbytes + (size_t)k0 * ESZ + c * 16);
-      *(uint4 *)(sA + tc::sw128_offset(r, c)) = v;
+
+  if (tid == 0) {
+    /* producer */
+    int i = 0;
+    for (; i < cnt; i++) {
+      const int s = i % stages;
+      if (i >= stages && !tc::mbar_wait(&empty[s], ((i / stages) - 1) & 1, kWaitTries)) {
+        s_fail = 1;
+        break;
+      }
+      uint8_t *sa = base + (size_t)s * STAGE;
+      tc::mbar_arrive_expect_tx(&full[s], STAGE);
+      tc::tma_load_2d(sa, &tmA, (kb0 + i) * EK, m0, &full[s]);
+      tc::tma_load_2d(sa + A_BYTES, &tmB, (kb0 + i) * EK, n0, &full[s]);
     }
-    for (int i = tid; i < BN * 8; i += 128) {
-      const int r = i >> 3, c = i & 7;
-      uint4 v = make_uint4(0, 0, 0, 0);
-      if (n0 + r < g.N) v = *(const uint4 *)(Bg + (size_t)(n0 + r) * rowbytes + (size_t)k0 * ESZ + c * 16);
-      *(uint4 *)(sB + tc::sw128_offset(r, c)) = v;
-    }
-    tc::fence_async_smem();
-    __syncthreads();
-    if (tid == 0) {
+    s_issued = i;
+  } else if (tid == 32) {
+    /* MMA issuer */
+    for (int i = 0; i < cnt; i++) {
+      const int s = i % stages;
+      if (!tc::mbar_wait(&full[s], (i / stages) & 1, kWaitTries)) {
+        s_fail = 1;
+        break;
+      }
       tc::fence_after_sync();
-      const uint32_t a0 = tc::smem_u32(sA), b0 = tc::smem_u32(sB);
+      const uint32_t a0 = tc::smem_u32(base + (size_t)s * STAGE), b0 = a0 + A_BYTES;
 #pragma unroll
       for (int j = 0; j < 4; j++) {
         const uint64_t ad = tc::smem_desc_sw128(a0 + 32 * j), bd = tc::smem_desc_sw128(b0 + 32 * j);
-        if (FP8) tc::mma_f8(taddr, ad, bd, IDESC, (k0 > 0 || j > 0) ? 1u : 0u);
-        else tc::mma_f16(taddr, ad, bd, IDESC, (k0 > 0 || j > 0) ? 1u : 0u);
+        if (FP8) tc::mma_f8(taddr, ad, bd, IDESC, (i > 0 || j > 0) ? 1u : 0u);
+        else tc::mma_f16(taddr, ad, bd, IDESC, (i > 0 || j > 0) ? 1u : 0u);
       }
-      tc::mma_commit(&bar);
+      tc::mma_commit(&empty[s]);
     }
-    /* the tiles may be overwritten only when the tensor cores are done */
-    ok &= tc::mbar_wait(&bar, phase, kWaitTries) ? 1 : 0;
-    phase ^= 1;
-    ok = __syncthreads_and(ok);
-    tc::fence_after_sync();
-    if (!ok) break;
+    tc::mma_commit(&done); /* arrives when every MMA above has completed */
   }
-  if (ok) {
+  const bool finished = tc::mbar_wait(&done, 0, kWaitTries);
+  __syncthreads();
+  tc::fence_after_sync();
+  if (finished && !s_fail) {
+    float scale = g.scale;
     if (g.amaxA && g.amaxB)
-      g.scale *= (__uint_as_float(*g.amaxA) / 448.f) * (__uint_as_float(*g.amaxB) / 448.f);
+      scale *= (__uint_as_float(*g.amaxA) / 448.f) * (__uint_as_float(*g.amaxB) / 448.f);
     const int row = m0 + warp * 32 + lane;
+    const bool split = gridDim.z > 1;
 #pragma unroll 1
     for (int c0 = 0; c0 < BN; c0 += 16) {
       float v[16];
       tc::tmem_ld16(taddr + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
-      if (row < g.M) {
+      const int cb = n0 + c0;
+      if (row >= g.M || cb >= g.N) continue;
+      const bool whole = cb + 16 <= g.N;
 #pragma unroll
-        for (int j = 0; j < 16; j++) {
-          const int col = n0 + c0 + j;
-          if (col >= g.N) continue;
-          float x = v[j] * g.scale;
-          if (g.bias) x += g.bias[col];
-          if (g.relu) x = fmaxf(x, 0.f);
-          if (g.mask && !(__bfloat162float(g.mask[(size_t)row * g.N + col]) > 0.f)) x = 0.f;
-          if (g.Cf) g.Cf[(size_t)row * g.N + col] = x;
-          if (g.Cb) g.Cb[(size_t)row * g.N + col] = __float2bfloat16(x);
-          if (g.Ct) g.Ct[(size_t)col * g.M + row] = __float2bfloat16(x);
+      for (int j = 0; j < 16; j++) {
+        float x = v[j] * scale;
+        if (g.bias && cb + j < g.N) x += g.bias[cb + j];
+        if (g.relu) x = fmaxf(x, 0.f);
+        v[j] = x;
+      }
+      if (g.mask) {
+        const bf16 *mk = g.mask + (size_t)row * g.N + cb;
+#pragma unroll
+        for (int j = 0; j < 16; j++)
+          if (cb + j < g.N && !(__bfloat162float(mk[j]) > 0.f)) v[j] = 0.f;
+      }
+      if (g.Cf) {
+        float *cp = g.Cf + (size_t)row * g.N + cb;
+        if (split) {
+#pragma unroll
+          for (int j = 0; j < 16; j++)
+            if (cb + j < g.N) atomicAdd(cp + j, v[j]);
+        } else if (whole && ((uintptr_t)cp & 15) == 0) {
+#pragma unroll
+          for (int j = 0; j < 16; j += 4) *(float4 *)(cp + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
+        } else {
+#pragma unroll
+          for (int j = 0; j < 16; j++)
+            if (cb + j < g.N) cp[j] = v[j];
         }
+      }
+      if (g.Cb) {
+        bf16 *cp = g.Cb + (size_t)row * g.N + cb;
+        if (whole && ((uintptr_t)cp & 15) == 0) {
+          __align__(16) bf16 h[16];
+#pragma unroll
+          for (int j = 0; j < 16; j++) h[j] = __float2bfloat16(v[j]);
+          *(uint4 *)cp = *(const uint4 *)h;
+          *(uint4 *)(cp + 8) = *(const uint4 *)(h + 8);
+        } else {
+#pragma unroll
+          for (int j = 0; j < 16; j++)
+            if (cb + j < g.N) cp[j] = __float2bfloat16(v[j]);
+        }
+      }
+      if (g.Ct) {
+#pragma unroll
+        for (int j = 0; j < 16; j++)
+          if (cb + j < g.N) g.Ct[(size_t)(cb + j) * g.M + row] = __float2bfloat16(v[j]);
       }
     }
   } else {
-    if (tid == 0) atomicOr(g.err, MST_TIMEOUT);
-    /* let the tensor cores drain (bounded) before the memory goes away */
-    tc::mbar_wait(&bar, phase ^ 1, kWaitTries);
+    if (tid == 0) {
+      atomicOr(g.err, MST_TIMEOUT);
+      /* copies still in flight land before the memory goes away */
+      const int issued = s_issued;
+      for (int i = max(0, issued - stages); i < issued; i++)
+        tc::mbar_wait(&full[i % stages], (i / stages) & 1, kWaitTries);
+    }
+    if (tid == 32) tc::mbar_wait(&done, 0, kWaitTries);
   }
   tc::fence_before_sync();
   __syncthreads();
   if (warp == 0) tc::tmem_free(taddr, BN);
 }
 
-constexpr size_t gemm_smem(int BN) { return 1024 + 16384 + (size_t)BN * 128; }
+/* driver's tensor-map encoder, looked up once through the runtime */
+PFN_cuTensorMapEncodeTiled_v12000 tmap_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+  }
+  return fn;
+}
+
+/* a K-major operand (rows x K) as a tensor map of 128-byte-wide boxes of
+ * box_rows rows, 128-byte swizzle; rows beyond the operand read as zero */
+int make_tmap(CUtensorMap *m, const void *ptr, uint64_t rows, uint64_t K, int esz, uint32_t box_rows) {
+  PFN_cuTensorMapEncodeTiled_v12000 enc = tmap_encoder();
+  if (!enc) return set_error(ZETA_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
+  if (((uintptr_t)ptr & 15) || ((K * esz) & 15)) return set_error(ZETA_ERR_ARG, "gemm operand not 16-byte aligned");
+  cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)K * esz};
+  cuuint32_t box[2] = {(cuuint32_t)(128 / esz), box_rows};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = enc(m, esz == 2 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_UINT8, 2,
+                   const_cast<void *>(ptr), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                   CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return set_error(ZETA_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+  return ZETA_OK;
+}
+
+constexpr size_t gemm_stage_bytes(int BN) { return (size_t)(128 + BN) * 128; }
+
+/* resident CTAs per SM the stage ring is sized for: 1 (deep ring) or 2
+ * (one CTA's epilogue overlaps the other's main loop) */
+int g_gemm_ctas_per_sm = 1;
 
 }  // namespace
 
+int gemm_set_ctas_per_sm(int c) {
+  if (c != 1 && c != 2) return set_error(ZETA_ERR_ARG, "gemm: CTAs per SM must be 1 or 2");
+  g_gemm_ctas_per_sm = c;
+  return ZETA_OK;
+}
+
 /* C = A . B^T (+bias, relu) on the tensor cores; operands K-major, K a
- * multiple of 64 (BF16) or 128 (FP8), N a multiple of 16. */
-int gemm_launch(const GemmArgs &g, bool fp8, cudaStream_t s) {
+ * multiple of 64 (BF16) or 128 (FP8), N a multiple of 16.  When only an
+ * FP32 output is written and the output is small next to K (weight
+ * gradients), the K range is split over CTAs that add their partial
+ * products atomically; the caller zeroes C first (accumulate = 1). */
+int gemm_launch(const GemmArgs &g, bool fp8, cudaStream_t s, int accumulate = 0) {
   if (g.M <= 0 || g.N <= 0 || g.K <= 0 || (g.K % (fp8 ? 128 : 64)) || (g.N % 16))
     return set_error(ZETA_ERR_ARG, "gemm: M %d N %d K %d not supported", g.M, g.N, g.K);
   const int BN = g.N >= 256 ? 256 : (g.N > 64 ? 128 : 64);
-  dim3 grid((g.M + 127) / 128, (g.N + BN - 1) / BN);
-  const size_t sm = gemm_smem(BN);
-  /* at most two CTAs per SM: their tensor memory (<= 256 columns each)
-   * always fits the SM's 512 columns, so no allocation ever waits */
-  const size_t sm_req = sm < 80 * 1024 ? 80 * 1024 : sm;
+  const int esz = fp8 ? 1 : 2;
+  CUtensorMap ta, tb;
+  int rc = make_tmap(&ta, g.A, (uint64_t)g.M, (uint64_t)g.K, esz, 128);
+  if (rc) return rc;
+  rc = make_tmap(&tb, g.B, (uint64_t)g.N, (uint64_t)g.K, esz, (uint32_t)BN);
+  if (rc) return rc;
+  const int mt = (g.M + 127) / 128, nt = (g.N + BN - 1) / BN;
+  const int nkb = g.K / (fp8 ? 128 : 64);
+  int splits = 1;
+  const bool plain_f32 = accumulate && g.Cf && !g.Cb && !g.Ct && !g.bias && !g.relu && !g.mask && !g.amaxA;
+  /* accumulate: 1 = C is zero already, 2 = zero it here when splitting */
+  if (plain_f32) {
+    const int sms = ctx().sms > 0 ? ctx().sms : 148;
+    while (mt * nt * splits * 2 <= sms && nkb / (splits * 2) >= 8) splits *= 2;
+  }
+  const int kbps = (nkb + splits - 1) / splits;
+  splits = (nkb + kbps - 1) / kbps;
+  if (splits > 1 && accumulate == 2) ZCHECK(cudaMemsetAsync(g.Cf, 0, (size_t)g.M * g.N * sizeof(float), s));
+  const size_t stage = gemm_stage_bytes(BN);
+  int stages = (int)((g_gemm_ctas_per_sm == 2 ? 110 * 1024 : 200 * 1024) / stage);
+  if (stages > kMaxStages) stages = kMaxStages;
+  if (stages > nkb) stages = nkb < 2 ? 2 : nkb;
+  const size_t smem = 1024 + (size_t)stages * stage;
+  dim3 grid(mt, nt, splits);
 #define ZETA_GEMM_CASE(BNV)                                                                              \
   if (BN == BNV) {                                                                                       \
     auto k = fp8 ? k_gemm<BNV, true> : k_gemm<BNV, false>;                                               \
-    ZCHECK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_req));            \
-    k<<<grid, 128, sm_req, s>>>(g);                                                                      \
+    ZCHECK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));              \
+    k<<<grid, 128, smem, s>>>(ta, tb, g, kbps, stages);                                                  \
   }
   ZETA_GEMM_CASE(64)
   ZETA_GEMM_CASE(128)
@@ -181,6 +323,8 @@ using namespace zeta;
 /* Test and tooling entry: C[M x N] (fp32) = A[M x K] . B[N x K]^T with
  * device buffers (bf16, or e4m3 when fp8 != 0).  Returns ZETA_ERR_BUDGET
  * when a tensor-core wait timed out. */
+extern "C" int zeta_gemm_configure(int ctas_per_sm) { return gemm_set_ctas_per_sm(ctas_per_sm); }
+
 extern "C" int zeta_gemm_tc(const void *d_A, const void *d_B, float *d_C, int M, int N, int K, int fp8, void *stream) {
   if (!d_A || !d_B || !d_C) return set_error(ZETA_ERR_ARG, "null buffer");
   static uint32_t *d_err = nullptr; /* one error word, kept for the process */
@@ -188,7 +332,7 @@ extern "C" int zeta_gemm_tc(const void *d_A, const void *d_B, float *d_C, int M,
   cudaStream_t s = (cudaStream_t)stream;
   ZCHECK(cudaMemsetAsync(d_err, 0, 4, s));
   GemmArgs g{d_A, d_B, M, N, K, nullptr, 0, d_C, nullptr, nullptr, 1.f, d_err, nullptr, nullptr, nullptr};
-  int rc = gemm_launch(g, fp8 != 0, s);
+  int rc = gemm_launch(g, fp8 != 0, s, 2);
   uint32_t err = 0;
   if (rc == ZETA_OK) {
     cudaError_t e = cudaMemcpyAsync(&err, d_err, 4, cudaMemcpyDeviceToHost, s);
@@ -564,16 +708,16 @@ int backward(MlpState &S, int n, int rows, cudaStream_t s) {
   if ((rc = gemm_launch(a, false, s))) return rc;
   GemmArgs b = gemm(S.dQt, S.H2t, kOut, kH2, rows, S.err); /* dW3 = dQ^T H2 */
   b.Cf = G + OFF_W3;
-  if ((rc = gemm_launch(b, false, s))) return rc;
+  if ((rc = gemm_launch(b, false, s, 1))) return rc; /* into the zeroed gradient */
   GemmArgs c = gemm(S.dH2, S.W2t, rows, kH1, kH2, S.err); /* dH1 = dH2 W2 . relu'(H1) */
   c.mask = S.H1, c.Cb = S.dH1, c.Ct = S.dH1t;
   if ((rc = gemm_launch(c, false, s))) return rc;
   GemmArgs d = gemm(S.dH2t, S.H1t, kH2, kH1, rows, S.err); /* dW2 = dH2^T H1 */
   d.Cf = G + OFF_W2;
-  if ((rc = gemm_launch(d, false, s))) return rc;
+  if ((rc = gemm_launch(d, false, s, 1))) return rc; /* into the zeroed gradient */
   GemmArgs e = gemm(S.dH1t, S.Xt, kH1, kIn, rows, S.err); /* dW1 = dH1^T X */
   e.Cf = G + OFF_W1;
-  if ((rc = gemm_launch(e, false, s))) return rc;
+  if ((rc = gemm_launch(e, false, s, 1))) return rc; /* into the zeroed gradient */
   k_colsum<<<(kOut + 127) / 128, 128, 0, s>>>(S.dQ, rows, kOut, G + OFF_B3);
   k_colsum<<<(kH2 + 127) / 128, 128, 0, s>>>(S.dH2, rows, kH2, G + OFF_B2);
   k_colsum<<<(kH1 + 127) / 128, 128, 0, s>>>(S.dH1, rows, kH1, G + OFF_B1);
