@@ -496,7 +496,7 @@ def run_gemm(args):
         for kind in ("bf16", "fp8"):
             best = min((1, 2), key=lambda c: res[f"{kind}_c{c}"]["ms"])
             res[kind] = dict(res[f"{kind}_c{best}"], ctas_per_sm=best)
-        z.gemm_configure(res["bf16"]["ctas_per_sm"])
+        z.gemm_configure(0)
         ref = (A.float() @ B.float().t())
         z.gemm_tc(A.data_ptr(), B.data_ptr(), C.data_ptr(), M, N, K, False, stream.cuda_stream)
         res["bf16_max_rel_err"] = float(((C - ref).abs().max() / ref.abs().max()).item())

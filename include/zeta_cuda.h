@@ -233,7 +233,8 @@ int zeta_mlp_scores(const uint64_t *boards, const uint8_t *stm, int n, int fp8, 
  * multiple of 16.  tcgen05.mma with FP32 accumulation in tensor memory. */
 int zeta_gemm_tc(const void *d_A, const void *d_B, float *d_C, int M, int N, int K, int fp8, void *stream);
 /* Tuning knob of that kernel: the shared-memory ring is sized for 1
- * (default, deepest pipeline) or 2 resident CTAs per SM. */
+ * (deepest pipeline) or 2 resident CTAs per SM; 0 (default) picks 2, or 1
+ * for split-K launches. */
 int zeta_gemm_configure(int ctas_per_sm);
 
 /* ------------------------------------------------------------------ */

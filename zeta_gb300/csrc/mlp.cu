@@ -258,13 +258,14 @@ int make_tmap(CUtensorMap *m, const void *ptr, uint64_t rows, uint64_t K, int es
 constexpr size_t gemm_stage_bytes(int BN) { return (size_t)(128 + BN) * 128; }
 
 /* resident CTAs per SM the stage ring is sized for: 1 (deep ring) or 2
- * (one CTA's epilogue overlaps the other's main loop) */
-int g_gemm_ctas_per_sm = 1;
+ * (one CTA's epilogue overlaps the other's main loop); 0 = choose: 2,
+ * except for split-K launches (few long-K tiles), which run best with 1 */
+int g_gemm_ctas_per_sm = 0;
 
 }  // namespace
 
 int gemm_set_ctas_per_sm(int c) {
-  if (c != 1 && c != 2) return set_error(ZETA_ERR_ARG, "gemm: CTAs per SM must be 1 or 2");
+  if (c < 0 || c > 2) return set_error(ZETA_ERR_ARG, "gemm: CTAs per SM must be 0 (auto), 1 or 2");
   g_gemm_ctas_per_sm = c;
   return ZETA_OK;
 }
@@ -297,7 +298,8 @@ int gemm_launch(const GemmArgs &g, bool fp8, cudaStream_t s, int accumulate = 0)
   splits = (nkb + kbps - 1) / kbps;
   if (splits > 1 && accumulate == 2) ZCHECK(cudaMemsetAsync(g.Cf, 0, (size_t)g.M * g.N * sizeof(float), s));
   const size_t stage = gemm_stage_bytes(BN);
-  int stages = (int)((g_gemm_ctas_per_sm == 2 ? 110 * 1024 : 200 * 1024) / stage);
+  const int ctas = g_gemm_ctas_per_sm ? g_gemm_ctas_per_sm : (splits > 1 ? 1 : 2);
+  int stages = (int)((ctas == 2 ? 110 * 1024 : 200 * 1024) / stage);
   if (stages > kMaxStages) stages = kMaxStages;
   if (stages > nkb) stages = nkb < 2 ? 2 : nkb;
   const size_t smem = 1024 + (size_t)stages * stage;
