@@ -26,15 +26,21 @@ MODEL = os.path.join(HERE, "models", "ordering_params.npy")
 TRAIN_SEED = 0x5A17A0000000004   # disjoint from the evaluation workloads' seeds
 
 
-def make_dataset(z, n: int, label_depth: int, seed: int = TRAIN_SEED, workers: int = 32):
-    """n positions (10-60 random plies) and the plain search's best move at label_depth."""
+def make_dataset(z, n: int, label_depth: int, seed: int = TRAIN_SEED, workers: int = 8, helpers: int = 32):
+    """n positions (10-60 random plies) and the plain search's best move at
+    label_depth, 8192 positions per launch (8 workers each, finished workers
+    help up to 32 per position: the fastest setting measured for labelling)."""
     boards, stm, _ = z.make_positions(seed, n, 10, 60, 0, 0, 0)
     best = np.zeros(n, dtype=np.uint32)
     chunk = 8192
-    for off in range(0, n, chunk):
-        z.tt_clear()
-        _, mv, _ = z.search_batch(boards[off:off + chunk], stm[off:off + chunk], label_depth, workers)
-        best[off:off + chunk] = mv
+    z.search_set_helpers(helpers)
+    try:
+        for off in range(0, n, chunk):
+            z.tt_clear()
+            _, mv, _ = z.search_batch(boards[off:off + chunk], stm[off:off + chunk], label_depth, workers)
+            best[off:off + chunk] = mv
+    finally:
+        z.search_set_helpers(0)
     return boards, stm, best
 
 
