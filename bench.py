@@ -438,6 +438,55 @@ def run_engine(args):
     z.release()
 
 
+def run_smp(args):
+    """The reference's own published search benchmark (results.txt,
+    `benchsmp`): the full engine's iterative deepening from the initial
+    position to depth 12, one position, fresh tables, with a growing number
+    of workers.  Metric: time to depth (s, lower is better); the best
+    published figure is 4.871 s (Titan RTX, 128 workers, results.txt:37)."""
+    import torch
+    import zeta_gb300 as z
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    z.init(local, 2048, 512)
+    depth = args.depth or 12
+    wlist = [args.workers] if args.workers else [64, 256, 1024, 4096, 16384]
+    b = z.STARTPOS
+    rows = []
+    with ClockSampler(local) as clocks:
+        for W in wlist:
+            z.tt_clear()
+            nodes, t0, launches = 0, time.perf_counter(), 0
+            for d in range(1, depth + 1):
+                pv, cnt = z.engine_search(b, 0, d, W)
+                launches += 1
+                nodes += int(cnt[:, 1].sum())
+                sc = int(np.int32(pv[0]))
+                if abs(sc) >= 30000 and d >= 32000 - abs(sc):
+                    break  # mate in n: no deeper iteration changes it
+            dt = time.perf_counter() - t0
+            rows.append({"workers": W, "seconds": round(dt, 3), "nps": round(nodes / dt, 1), "nodes": nodes,
+                         "score": sc, "move": int(pv[1]), "launches": launches})
+            print(json.dumps(rows[-1]), file=sys.stderr, flush=True)
+    best = min(rows, key=lambda r: r["seconds"])
+    if rank == 0:
+        print(json.dumps({
+            "metric": f"full-engine time to depth {depth} from the initial position (reference benchsmp)",
+            "value": best["seconds"], "unit": "s", "n_gpus": world, "steps": 1, "warmup": 0,
+            "ms_per_step": round(best["seconds"] * 1e3, 1), "higher_is_better": False, "scaling": "replicas",
+            "vs_baseline": round(best["seconds"] / 4.871, 4) if depth == 12 else None,
+            "baseline": "4.871 s: Titan RTX, 128 work-groups, version 099k (results.txt:37)",
+            "dtype": "int32", "data": "the initial position",
+            "config": {"workload": f"startpos iterative deepening 1..{depth}, 2 GB TT1 + 512 MB TT2, fresh tables",
+                       "workers": best["workers"]},
+            "nodes_per_s": best["nps"],
+            "e2e": {"value": best["seconds"], "unit": "s", "h2d_bytes_per_step": 58 * best["launches"],
+                    "d2h_bytes_per_step": (256 + 512 * best["workers"]) * best["launches"]},
+            "gpu_launches": best["launches"], "clocks": clocks.summary(), "scaling_table": rows,
+        }), flush=True)
+    z.release()
+
+
 GEMM_SHAPES = (
     # (M, N, K): the move-ordering network's layers at a 65536-position batch
     (65536, 512, 768),   # forward layer 1 (768 one-hot -> 512)
@@ -568,7 +617,8 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--n", type=int, default=0, help="positions per GPU (default: the workload's 4096)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the timed CPU baseline (profiling runs)")
-    ap.add_argument("--workload", choices=["perft_batch", "search_batch", "gemm", "engine"], default="perft_batch")
+    ap.add_argument("--workload", choices=["perft_batch", "search_batch", "gemm", "engine", "smp"],
+                    default="perft_batch")
     ap.add_argument("--depth", type=int, default=0, help="search depth (search_batch; default 7)")
     ap.add_argument("--workers", type=int, default=0, help="ABDADA workers per position (0 = sweep)")
     ap.add_argument("--helpers", type=int, default=0, help="helper cap: max workers per position (0 = none)")
@@ -581,6 +631,8 @@ def main():
         run_gemm(args)
     elif args.workload == "engine" and args.impl == "ours":
         run_engine(args)
+    elif args.workload == "smp" and args.impl == "ours":
+        run_smp(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -12,13 +12,22 @@ namespace zeta {
 
 namespace {
 
+/* One worker per thread (dense: 32 workers of different trees share a
+ * warp, the most workers resident) or one worker per warp (sparse: lane 0
+ * of each warp works alone, so a worker never waits for the other paths
+ * of its warp; used when all workers fit on the GPU at once, as in a
+ * single-position search). */
 template <int TPB>
-__global__ void __launch_bounds__(TPB) k_engine(EngineArgs a) {
+__global__ void __launch_bounds__(TPB) k_engine(EngineArgs a, int sparse) {
   __shared__ EvalTables sT;
   for (int i = threadIdx.x; i < (int)(sizeof(EvalTables) / 4); i += TPB)
     ((uint32_t *)&sT)[i] = ((const uint32_t *)&kEvalDev)[i];
   __syncthreads();
-  const long long t = (long long)blockIdx.x * TPB + threadIdx.x;
+  long long t = (long long)blockIdx.x * TPB + threadIdx.x;
+  if (sparse) {
+    if (threadIdx.x & 31) return;
+    t >>= 5;
+  }
   if (t >= (long long)a.N * a.W) return;
   engine_worker(a, t, sT);
 }
@@ -190,9 +199,18 @@ int engine_launch(int n, int w, int depth, uint64_t max_nodes, bool with_hist, b
   ZCHECK(cudaMemsetAsync(e.pv, 0, (size_t)n * kEPly * sizeof(uint32_t), c.stream));
   ZCHECK(cudaMemsetAsync(e.status, 0, sizeof(uint32_t), c.stream));
   const long long total = (long long)n * w;
-  const int blocks = (int)((total + kEngineTPB - 1) / kEngineTPB);
+  /* sparse when every worker can have a resident warp of its own */
+  static int resident_blocks = 0;
+  if (!resident_blocks) {
+    int per_sm = 0;
+    ZCHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_engine<kEngineTPB>, kEngineTPB, 0));
+    resident_blocks = (per_sm > 0 ? per_sm : 1) * c.sms;
+  }
+  const int sparse = total <= (long long)resident_blocks * (kEngineTPB / 32) ? 1 : 0;
+  const long long threads = sparse ? total * 32 : total;
+  const int blocks = (int)((threads + kEngineTPB - 1) / kEngineTPB);
   ZCHECK(cudaEventRecord(c.ev[0], c.stream));
-  k_engine<kEngineTPB><<<blocks, kEngineTPB, 0, c.stream>>>(a);
+  k_engine<kEngineTPB><<<blocks, kEngineTPB, 0, c.stream>>>(a, sparse);
   ZCHECK(cudaGetLastError());
   ZCHECK(cudaEventRecord(c.ev[1], c.stream));
   ZCHECK(cudaStreamSynchronize(c.stream));

@@ -92,6 +92,52 @@ void perft(Bitboard *board, int stm, int depth) {
   for (uint64_t i = 0; i < totalWorkUnits; i++) ABNODECOUNT += COUNTERS[i * 64 + 1];
 }
 
+/* Worker-scaling benchmark (the reference's `benchsmp`, src/xboard.c:822-974):
+ * the same iterative-deepening search to `depth` with 1, 2, 4, ... workers
+ * up to max_workers, each run from fresh tables, then one table of nodes
+ * per second, time-to-depth and the speedups over 1 worker and over the
+ * previous worker count, in the reference's results.txt layout. */
+void benchsmp(Bitboard *board, int stm, int depth, uint64_t max_workers) {
+  enum { kMaxRuns = 40 };
+  double secs[kMaxRuns];
+  uint64_t nps[kMaxRuns], workers[kMaxRuns];
+  int runs = 0;
+  const uint64_t saved = totalWorkUnits;
+  if (max_workers < 1) max_workers = 1;
+  for (uint64_t w = 1; runs < kMaxRuns;) {
+    printf("### doing inits for benchsmp depth %d: ###\n", depth);
+    totalWorkUnits = w;
+    engine_free();
+    if (!engine_alloc()) die();
+    if (!cl_release_device() || !cl_init_device("alphabeta_gpu")) die(); /* fresh tables */
+    printf("### computing benchsmp depth %d: ###\n", depth);
+    printf("### work-groups: %" PRIu64 " ###\n", w);
+    double t0 = get_time_ms();
+    rootsearch(board, stm, depth);
+    double el = (get_time_ms() - t0 + 1.0) / 1000.0;
+    secs[runs] = el;
+    nps[runs] = (uint64_t)((double)ABNODECOUNT / el);
+    workers[runs] = w;
+    runs++;
+    if (w >= max_workers) break;
+    w = w * 2 > max_workers ? max_workers : w * 2;
+  }
+  printf("### workers\t#nps\t\t#nps speedup\t#time in s\t#ttd speedup \t#relative ttd speedup ###\n");
+  for (int i = 0; i < runs; i++) {
+    const double ns = nps[0] ? (double)nps[i] / (double)nps[0] : 0.0;
+    const double ttd = secs[0] / secs[i], rel = i ? secs[i - 1] / secs[i] : 1.0;
+    printf("### %" PRIu64 "\t\t%" PRIu64 "\t\t%lf\t%lf\t%lf\t%lf \n", workers[i], nps[i], ns, secs[i], ttd, rel);
+    if (LogFile)
+      fprintf(LogFile, "### %" PRIu64 "\t\t%" PRIu64 "\t\t%lf\t%lf\t%lf\t%lf \n", workers[i], nps[i], ns, secs[i],
+              ttd, rel);
+  }
+  totalWorkUnits = saved;
+  engine_free();
+  if (!engine_alloc()) die();
+  if (!cl_release_device() || !cl_init_device("alphabeta_gpu")) die();
+  fflush(stdout);
+}
+
 /* The 14 known-answer tests of the reference's selftest (src/test.c:43-73). */
 int selftest(void) {
   static const char *fens[4] = {

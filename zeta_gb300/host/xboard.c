@@ -107,6 +107,10 @@ void xboard(void) {
       if (!cl_release_device() || !cl_init_device("alphabeta_gpu")) exit(EXIT_FAILURE);
     } else if (!strcmp(cmd, "selftest") && !xboard_mode) {
       selftest();
+    } else if (!strcmp(cmd, "benchsmp") && !xboard_mode) {
+      /* benchsmp [max workers]: worker scaling of the search to depth sd */
+      uint64_t maxw = strtoull(arg, NULL, 10);
+      benchsmp(BOARD, STM, SD, maxw ? maxw : totalWorkUnits);
     } else if (!strcmp(cmd, "print") && !xboard_mode) {
       char fen[256];
       board_print(BOARD, STM);
@@ -114,7 +118,7 @@ void xboard(void) {
       printf("# %s\n", fen);
     } else if (!strcmp(cmd, "help") && !xboard_mode) {
       printf("# commands: new, setboard <fen>, go, usermove <move>, force, sd <depth>, perft <depth>,\n"
-             "# selftest, print, quit (and the xboard protocol)\n");
+             "# benchsmp [max workers], selftest, print, quit (and the xboard protocol)\n");
     } else if (!strcmp(cmd, "accepted") || !strcmp(cmd, "rejected") || !strcmp(cmd, "level") ||
                !strcmp(cmd, "st") || !strcmp(cmd, "time") || !strcmp(cmd, "otim") || !strcmp(cmd, "random") ||
                !strcmp(cmd, "computer") || !strcmp(cmd, "result") || !strcmp(cmd, "hard") ||

@@ -9,7 +9,7 @@
    with the network's ordering (BF16 or FP8) on the same positions; the
    root scores must be identical, nodes and time-to-depth are compared.
 
-    python -m zeta_gb300.learn train [--n 131072] [--label-depth 5] [--epochs 10]
+    python -m zeta_gb300.learn train [--n 524288] [--label-depth 6] [--epochs 20]
     python -m zeta_gb300.learn ab [--n 1024] [--depth 8]
 """
 from __future__ import annotations
@@ -94,8 +94,8 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("cmd", choices=["train", "ab"])
     ap.add_argument("--n", type=int, default=0)
-    ap.add_argument("--label-depth", type=int, default=5)
-    ap.add_argument("--epochs", type=int, default=10)
+    ap.add_argument("--label-depth", type=int, default=6)
+    ap.add_argument("--epochs", type=int, default=20)
     ap.add_argument("--depth", type=int, default=8)
     ap.add_argument("--workers", type=int, default=32)
     ap.add_argument("--out", default="")
@@ -104,7 +104,7 @@ def main():
     a = ap.parse_args()
     z.init(0, 1024, 0)
     if a.cmd == "train":
-        n = a.n or 131072
+        n = a.n or 524288
         t0 = time.time()
         boards, stm, best = make_dataset(z, n, a.label_depth)
         t1 = time.time()
