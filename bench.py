@@ -448,9 +448,9 @@ def run_smp(args):
     import zeta_gb300 as z
     world, rank, local = dist_env()
     torch.cuda.set_device(local)
-    z.init(local, 2048, 512)
+    z.init(local, 2048, args.tt2_mb)
     depth = args.depth or 12
-    wlist = [args.workers] if args.workers else [64, 256, 1024, 4096, 16384]
+    wlist = [args.workers] if args.workers else [32, 64, 128, 256, 512]
     b = z.STARTPOS
     rows = []
     with ClockSampler(local) as clocks:
@@ -477,7 +477,8 @@ def run_smp(args):
             "vs_baseline": round(best["seconds"] / 4.871, 4) if depth == 12 else None,
             "baseline": "4.871 s: Titan RTX, 128 work-groups, version 099k (results.txt:37)",
             "dtype": "int32", "data": "the initial position",
-            "config": {"workload": f"startpos iterative deepening 1..{depth}, 2 GB TT1 + 512 MB TT2, fresh tables",
+            "config": {"workload": f"startpos iterative deepening 1..{depth}, 2 GB TT1 + {args.tt2_mb} MB TT2, "
+                                   "fresh tables",
                        "workers": best["workers"]},
             "nodes_per_s": best["nps"],
             "e2e": {"value": best["seconds"], "unit": "s", "h2d_bytes_per_step": 58 * best["launches"],
@@ -622,6 +623,8 @@ def main():
     ap.add_argument("--depth", type=int, default=0, help="search depth (search_batch; default 7)")
     ap.add_argument("--workers", type=int, default=0, help="ABDADA workers per position (0 = sweep)")
     ap.add_argument("--helpers", type=int, default=0, help="helper cap: max workers per position (0 = none)")
+    ap.add_argument("--tt2-mb", type=int, default=512,
+                    help="smp: ABDADA table size (0 = no TT2: helpers randomise their move order instead)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

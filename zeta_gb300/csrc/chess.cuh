@@ -462,10 +462,10 @@ ZHD int emit_shift(const Pos &p, int stm, u64 t, int delta, Move *list, int n) {
   return n;
 }
 
-ZHD int gen_legal(const Pos &p, int stm, bool qs, Move *list) {
-  Sets s = make_sets(p, stm);
+/* the same with the side's piece sets and the enemy attack map already
+ * computed (callers that also need the in-check test) */
+ZHD int gen_legal_sd(const Pos &p, const Sets &s, u64 danger, int stm, bool qs, Move *list) {
   Guard g = make_guard(s, stm);
-  u64 danger = enemy_attacks(s, stm);
   u64 capmask = qs ? s.them : ~0ULL;
   u64 tgt = ~s.us & g.cmask & capmask;
   int n = 0;
@@ -534,6 +534,11 @@ ZHD int gen_legal(const Pos &p, int stm, bool qs, Move *list) {
     if (e & 2) list[n++] = make_move(sqep + 1, to, sqep, pawn, pawn, victim);
   }
   return n;
+}
+
+ZHD int gen_legal(const Pos &p, int stm, bool qs, Move *list) {
+  const Sets s = make_sets(p, stm);
+  return gen_legal_sd(p, s, enemy_attacks(s, stm), stm, qs, list);
 }
 
 }  // namespace zeta
