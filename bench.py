@@ -450,36 +450,47 @@ def run_smp(args):
     torch.cuda.set_device(local)
     z.init(local, 2048, args.tt2_mb)
     depth = args.depth or 12
-    wlist = [args.workers] if args.workers else [32, 64, 128, 256, 512]
+    wlist = [args.workers] if args.workers else [64, 128, 256, 512, 1024]
     b = z.STARTPOS
+
+    def run(W):
+        z.tt_clear()
+        nodes, t0, launches, sc, pv = 0, time.perf_counter(), 0, 0, None
+        for d in range(1, depth + 1):
+            pv, cnt = z.engine_search(b, 0, d, W)
+            launches += 1
+            nodes += int(cnt[:, 1].sum())
+            sc = int(np.int32(pv[0]))
+            if abs(sc) >= 30000 and d >= 32000 - abs(sc):
+                break  # mate in n: no deeper iteration changes it
+        dt = time.perf_counter() - t0
+        return {"workers": W, "seconds": round(dt, 3), "nps": round(nodes / dt, 1), "nodes": nodes, "score": sc,
+                "move": int(pv[1]), "launches": launches}
+
     rows = []
     with ClockSampler(local) as clocks:
-        for W in wlist:
-            z.tt_clear()
-            nodes, t0, launches = 0, time.perf_counter(), 0
-            for d in range(1, depth + 1):
-                pv, cnt = z.engine_search(b, 0, d, W)
-                launches += 1
-                nodes += int(cnt[:, 1].sum())
-                sc = int(np.int32(pv[0]))
-                if abs(sc) >= 30000 and d >= 32000 - abs(sc):
-                    break  # mate in n: no deeper iteration changes it
-            dt = time.perf_counter() - t0
-            rows.append({"workers": W, "seconds": round(dt, 3), "nps": round(nodes / dt, 1), "nodes": nodes,
-                         "score": sc, "move": int(pv[1]), "launches": launches})
+        for W in wlist:  # the worker sweep (benchsmp's table)
+            rows.append(run(W))
             print(json.dumps(rows[-1]), file=sys.stderr, flush=True)
-    best = min(rows, key=lambda r: r["seconds"])
+        # multi-worker searches vary run to run: repeat the fastest count
+        w_best = min(rows, key=lambda r: r["seconds"])["workers"]
+        reps = [run(w_best) for _ in range(max(1, args.steps))]
+        for r in reps:
+            print(json.dumps(dict(r, repeat=True)), file=sys.stderr, flush=True)
+    reps.sort(key=lambda r: r["seconds"])
+    best = reps[len(reps) // 2]  # the median run
     if rank == 0:
         print(json.dumps({
             "metric": f"full-engine time to depth {depth} from the initial position (reference benchsmp)",
-            "value": best["seconds"], "unit": "s", "n_gpus": world, "steps": 1, "warmup": 0,
+            "value": best["seconds"], "unit": "s", "n_gpus": world, "steps": len(reps), "warmup": 0,
             "ms_per_step": round(best["seconds"] * 1e3, 1), "higher_is_better": False, "scaling": "replicas",
             "vs_baseline": round(best["seconds"] / 4.871, 4) if depth == 12 else None,
             "baseline": "4.871 s: Titan RTX, 128 work-groups, version 099k (results.txt:37)",
             "dtype": "int32", "data": "the initial position",
             "config": {"workload": f"startpos iterative deepening 1..{depth}, 2 GB TT1 + {args.tt2_mb} MB TT2, "
                                    "fresh tables",
-                       "workers": best["workers"]},
+                       "workers": best["workers"], "statistic": f"median of {len(reps)} runs",
+                       "runs_s": [r["seconds"] for r in reps]},
             "nodes_per_s": best["nps"],
             "e2e": {"value": best["seconds"], "unit": "s", "h2d_bytes_per_step": 58 * best["launches"],
                     "d2h_bytes_per_step": (256 + 512 * best["workers"]) * best["launches"]},
@@ -623,7 +634,7 @@ def main():
     ap.add_argument("--depth", type=int, default=0, help="search depth (search_batch; default 7)")
     ap.add_argument("--workers", type=int, default=0, help="ABDADA workers per position (0 = sweep)")
     ap.add_argument("--helpers", type=int, default=0, help="helper cap: max workers per position (0 = none)")
-    ap.add_argument("--tt2-mb", type=int, default=512,
+    ap.add_argument("--tt2-mb", type=int, default=0,
                     help="smp: ABDADA table size (0 = no TT2: helpers randomise their move order instead)")
     args = ap.parse_args()
     if args.warmup < 3:

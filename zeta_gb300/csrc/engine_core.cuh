@@ -199,6 +199,16 @@ ZE void tt2_store(TT2E *p, const TT2E &e) {
 #endif
 }
 
+/* start moving a table entry into L2 (the child's entry, probed when the
+ * child is entered); no effect on host builds */
+ZE void prefetch_l2(const void *p) {
+#if defined(__CUDA_ARCH__)
+  asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+#else
+  (void)p;
+#endif
+}
+
 /* 32-bit atomics of the ABDADA table and the early-bird flag */
 ZE int e_cas(int *p, int cmp, int val) {
 #if defined(__CUDA_ARCH__)
@@ -826,6 +836,8 @@ __host__ __device__ void engine_worker(const EngineArgs &a, long long t, const E
     c->th = th;
     const u64 h = th ^ (move == E_NULLMOVE ? 1ULL : 0ULL); /* the null move toggles once more */
     c->hash = h;
+    if (tt1) prefetch_l2(tt1 + (h & mask1));
+    if (tt2) prefetch_l2(tt2 + (h & mask2));
     if (ply + ply_init < kGamePly) H[ply + ply_init] = h;
     c->hmc = (uint8_t)next_hmc(g->hmc, move);
     c->mh = 0;
