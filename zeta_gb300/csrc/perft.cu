@@ -39,6 +39,7 @@ namespace {
 
 constexpr uint32_t ST_CAPACITY = 1u;
 constexpr uint32_t ST_DEPTH = 2u;
+constexpr uint32_t ST_BOUNDS = 4u; /* a write fell outside its buffer: skipped, reported */
 constexpr int kMaxChildren = 218; /* most legal moves of any chess position */
 
 __device__ __forceinline__ Pos load_pos(const uint64_t *b) {
@@ -76,7 +77,9 @@ __global__ void k_roots(const uint64_t *__restrict__ boards, const uint8_t *__re
 __global__ void __launch_bounds__(128) k_split(int level, const Task *__restrict__ in, Task *__restrict__ out,
                                                Task *__restrict__ fin, uint32_t cap_lvl, uint32_t cap_fin,
                                                uint32_t min_tasks, int rmax, PerftCounters *pc) {
-  const uint32_t n_in = pc->level_n[level];
+  /* a level that overflowed its array counted past it (and flagged
+   * ST_CAPACITY): read only what was stored */
+  const uint32_t n_in = min(pc->level_n[level], cap_lvl);
   const bool last = level == kMaxLevels - 1;
   Move list[256];
   unsigned long long interior = 0;
@@ -185,8 +188,8 @@ __device__ __noinline__ int expand_node(Pos p, int stm, Move *list) { return gen
  * children of a node contiguous; returns the number written.  Block-wide:
  * every thread must call it. */
 template <int TPB>
-__device__ __forceinline__ int expand_round(const Pos *src, int nsrc, int stm, Pos *dst, int *s_warp, Move *list,
-                                            unsigned long long &interior) {
+__device__ __forceinline__ int expand_round(const Pos *src, int nsrc, int stm, Pos *dst, int dst_cap, int *s_warp,
+                                            Move *list, unsigned long long &interior, uint32_t *status) {
   const int tid = threadIdx.x;
   int k = 0;
   if (tid < nsrc) {
@@ -195,13 +198,17 @@ __device__ __forceinline__ int expand_round(const Pos *src, int nsrc, int stm, P
   }
   int off;
   const int total = block_exclusive_scan<TPB>(k, off, s_warp);
+  if (off + k > dst_cap) {
+    atomicOr(status, ST_BOUNDS);
+    k = off < dst_cap ? dst_cap - off : 0;
+  }
   for (int j = 0; j < k; j++) {
     Pos c = src[tid];
     play(c, list[j], true);
     dst[off + j] = c;
   }
   __syncthreads();
-  return total;
+  return total < dst_cap ? total : dst_cap;
 }
 
 /* sum of the legal-move counts of src[0..n): the leaf count below them */
@@ -222,7 +229,8 @@ __device__ __forceinline__ unsigned long long count_range(const Pos *src, int n,
 template <int TPB, int MINB>
 __global__ void __launch_bounds__(TPB, MINB) k_perft_ws(const Task *__restrict__ tasks, uint32_t *cursors,
                                                   uint64_t *__restrict__ leaves, PerftCounters *pc,
-                                                  Pos *__restrict__ scratch, uint32_t cap2, uint32_t cap3) {
+                                                  Pos *__restrict__ scratch, uint32_t cap2, uint32_t cap3,
+                                                  uint32_t cap_fin, uint32_t n_roots) {
   __shared__ Pos s_l1[256];
   __shared__ Pos s_root;
   __shared__ int s_warp[TPB / 32];
@@ -230,7 +238,7 @@ __global__ void __launch_bounds__(TPB, MINB) k_perft_ws(const Task *__restrict__
   __shared__ uint32_t s_task;
 
   const int tid = threadIdx.x;
-  const uint32_t n = pc->n_final;
+  const uint32_t n = min(pc->n_final, cap_fin); /* tasks beyond the array were not stored */
   const uint32_t B = gridDim.x;
   const int per_round = min(TPB, (int)(cap3 / kMaxChildren));
   Pos *b2 = scratch + (size_t)blockIdx.x * (cap2 + cap3);
@@ -258,7 +266,7 @@ __global__ void __launch_bounds__(TPB, MINB) k_perft_ws(const Task *__restrict__
       acc = count_range<TPB>(&s_root, 1, t.stm, counted);
     } else {
       /* level 1: the task root's children, in shared memory */
-      const int n1 = expand_round<TPB>(&s_root, 1, t.stm, s_l1, s_warp, list, interior);
+      const int n1 = expand_round<TPB>(&s_root, 1, t.stm, s_l1, 256, s_warp, list, interior, &pc->status);
       if (R == 2) {
         acc = count_range<TPB>(s_l1, n1, t.stm ^ 1, counted);
       } else {
@@ -268,22 +276,26 @@ __global__ void __launch_bounds__(TPB, MINB) k_perft_ws(const Task *__restrict__
         if (R == 4) {
           int n2 = 0;
           for (int base = 0; base < n1; base += TPB)
-            n2 += expand_round<TPB>(s_l1 + base, min(TPB, n1 - base), t.stm ^ 1, b2 + n2, s_warp, list, interior);
+            n2 += expand_round<TPB>(s_l1 + base, min(TPB, n1 - base), t.stm ^ 1, b2 + n2, (int)cap2 - n2, s_warp,
+                                    list, interior, &pc->status);
           par = b2;
           npar = n2;
           spar = t.stm;
         }
         /* the nodes one ply above the leaves, a round at a time, then count */
         for (int base = 0; base < npar; base += per_round) {
-          const int total = expand_round<TPB>(par + base, min(per_round, npar - base), spar, b3, s_warp, list,
-                                              interior);
+          const int total = expand_round<TPB>(par + base, min(per_round, npar - base), spar, b3, (int)cap3, s_warp,
+                                              list, interior, &pc->status);
           acc += count_range<TPB>(b3, total, spar ^ 1, counted);
           __syncthreads();
         }
       }
     }
     const unsigned long long sum = block_sum<TPB>(acc, s_red);
-    if (tid == 0 && sum) atomicAdd((unsigned long long *)&leaves[t.root], sum);
+    if (tid == 0 && sum) {
+      if (t.root < n_roots) atomicAdd((unsigned long long *)&leaves[t.root], sum);
+      else atomicOr(&pc->status, ST_BOUNDS);
+    }
   }
   /* warp-aggregate the statistics */
   for (int o = 16; o > 0; o >>= 1) {
@@ -309,7 +321,8 @@ __global__ void k_genmoves(const uint64_t *__restrict__ boards, const uint8_t *_
   for (int j = 0; j < k; j++) moves[(size_t)i * 256 + j] = list[j];
 }
 
-typedef void (*WsKernel)(const Task *, uint32_t *, uint64_t *, PerftCounters *, Pos *, uint32_t, uint32_t);
+typedef void (*WsKernel)(const Task *, uint32_t *, uint64_t *, PerftCounters *, Pos *, uint32_t, uint32_t,
+                         uint32_t, uint32_t);
 
 /* Compiled variants: threads per block x minimum resident blocks per SM
  * (the second number caps registers per thread at 65536/(TPB*MINB));
@@ -409,7 +422,8 @@ static int perft_enqueue(const uint64_t *d_boards, const uint8_t *d_stm, const u
    * nodes of the graph, so the kernel is timed on every replay */
   ZCHECK(capturing ? cudaEventRecordWithFlags(c.ev[1], s, cudaEventRecordExternal) : cudaEventRecord(c.ev[1], s));
   const uint32_t cap2 = c.pcfg.task_depth >= 4 ? (uint32_t)(kMaxChildren * kMaxChildren) : 0u;
-  k<<<blocks, tpb, 0, s>>>(c.fin, c.cursors, d_leaves, c.pc, c.scratch, cap2, (uint32_t)tpb * kMaxChildren);
+  k<<<blocks, tpb, 0, s>>>(c.fin, c.cursors, d_leaves, c.pc, c.scratch, cap2, (uint32_t)tpb * kMaxChildren,
+                           c.cap_fin, (uint32_t)n);
   ZCHECK(cudaGetLastError());
   ZCHECK(capturing ? cudaEventRecordWithFlags(c.ev[2], s, cudaEventRecordExternal) : cudaEventRecord(c.ev[2], s));
   return ZETA_OK;
@@ -445,8 +459,8 @@ int perft_run(const uint64_t *d_boards, const uint8_t *d_stm, const uint8_t *d_d
   WsKernel k;
   int rc = ws_geometry(blocks, tpb, k);
   if (rc) return rc;
-  if (c.cap_fin == 0) {
-    rc = perft_ensure_arena(8u << 20);
+  if (c.cap_fin == 0 || (uint32_t)n > c.cap_lvl) {
+    rc = perft_ensure_arena(std::max<uint64_t>(8u << 20, (uint64_t)n + n / 4)); /* the roots fit level 0 */
     if (rc) return rc;
   }
   ZCHECK(cudaEventRecord(c.ev[0], s));
@@ -503,6 +517,7 @@ int perft_run(const uint64_t *d_boards, const uint8_t *d_stm, const uint8_t *d_d
                      (unsigned long long)need);
   }
   if (h.status & ST_DEPTH) return set_error(ZETA_ERR_ARG, "perft depth above %d", kMaxDepth);
+  if (h.status & ST_BOUNDS) return set_error(ZETA_ERR_DEVICE, "perft: a buffer bound was hit (write skipped)");
   return ZETA_OK;
 }
 
@@ -588,7 +603,7 @@ extern "C" int zeta_perft_batch_noalloc(const uint64_t *d_boards, const uint8_t 
     ZCHECK(cudaGetLastError());
   }
   k_perft_ws<128, 1><<<blocks, 128, 0, s>>>(S->fin, S->cursors, d_leaves, &S->pc, S->nodes, 0u,
-                                            kNoAllocNodesPerBlock);
+                                            kNoAllocNodesPerBlock, kNoAllocMaxTasks, (uint32_t)n);
   ZCHECK(cudaGetLastError());
   uint32_t status = 0;
   ZCHECK(cudaMemcpyAsync(&status, &S->pc.status, sizeof status, cudaMemcpyDeviceToHost, s));
@@ -596,5 +611,6 @@ extern "C" int zeta_perft_batch_noalloc(const uint64_t *d_boards, const uint8_t 
   if (status & ST_CAPACITY)
     return set_error(ZETA_ERR_NOALLOC, "the split needs more than %u subtree tasks (fixed scratch)", kNoAllocMaxTasks);
   if (status & ST_DEPTH) return set_error(ZETA_ERR_ARG, "perft depth above %d", kMaxDepth);
+  if (status & ST_BOUNDS) return set_error(ZETA_ERR_DEVICE, "perft: a buffer bound was hit (write skipped)");
   return ZETA_OK;
 }
