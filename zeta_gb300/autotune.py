@@ -23,8 +23,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 TUNED = os.path.join(HERE, "perft_tuned.json")
 
 # (threads_per_block, blocks_per_sm) pairs compiled into libzeta_cuda.so
-VARIANTS = [(64, 0), (64, 8), (64, 12), (128, 0), (128, 4), (128, 6), (128, 8), (256, 0), (256, 3), (256, 4),
-            (512, 0), (512, 2)]
+VARIANTS = [(64, 0), (64, 8), (64, 12), (128, 0), (128, 4), (128, 6), (256, 0), (256, 3), (512, 0)]
 TASK_DEPTHS = (3, 4)
 
 
