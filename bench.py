@@ -335,7 +335,7 @@ def run_search(args):
     # (workers per position, helper cap): helpers let finished workers join
     # unfinished positions up to `cap` workers each (0 = no helping)
     workers_list = ([(args.workers, args.helpers)] if args.workers else
-                    [(32, 0), (64, 0), (16, 48), (32, 64), (32, 96)])
+                    [(1, 16), (1, 32), (16, 48), (32, 96), (32, 128)])
     results = {}
     ref_scores = None
     for W, cap in workers_list:

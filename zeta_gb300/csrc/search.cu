@@ -38,6 +38,7 @@
 
 #include "context.cuh"
 #include "eval.cuh"
+#include "movegen_fast.cuh"
 #include "tables.cuh"
 
 namespace zeta {
@@ -61,8 +62,8 @@ enum Bound : uint32_t { B_NONE = 0, B_LOWER = 1, B_UPPER = 2, B_EXACT = 3 };
 /* exact castle rights and the en-passant square mixed into the reference
  * Zobrist hash: its castle keys depend on either of the king and rook
  * flags, which two positions with different rights can share */
-__device__ __forceinline__ u64 search_key(const Pos &p, int stm) {
-  u64 k = compute_hash(p, stm);
+__device__ __forceinline__ u64 search_key(const Pos &p, u64 hash) {
+  u64 k = hash; /* the reference hash of (p, side to move) */
   u64 cr = ~p.cr;
   uint32_t rights = ((cr & ZETA_CR_WQ) == ZETA_CR_WQ) | (((cr & ZETA_CR_WK) == ZETA_CR_WK) << 1) |
                     (((cr & ZETA_CR_BQ) == ZETA_CR_BQ) << 2) | (((cr & ZETA_CR_BK) == ZETA_CR_BK) << 3);
@@ -117,6 +118,7 @@ __device__ __forceinline__ int order_score(Move m, int stm, Move ttmove, Move k0
 /* one ply of a worker's explicit stack */
 struct Frame {
   Pos pos;
+  u64 th; /* reference Zobrist hash of (pos, stm), updated move by move */
   u64 key;
   int alpha, beta, alpha0, best;
   Move bestmove;
@@ -141,7 +143,10 @@ __device__ __noinline__ int s_count(Pos p, int stm, bool *chk) {
   *chk = c;
   return n;
 }
-__device__ __noinline__ int s_gen(Pos p, int stm, Move *list) { return gen_legal(p, stm, false, list); }
+__device__ __noinline__ int s_gen(Pos p, int stm, Move *list) {
+  const Sets s = make_sets(p, stm);
+  return gen_engine(p, s, enemy_attacks(s, stm), stm, false, list);
+}
 __device__ __noinline__ int s_eval(Pos p, const EvalTables *T) { return eval_white(p, *T); }
 
 /* value of a node with no depth left, from the side to move */
@@ -195,7 +200,7 @@ __device__ __forceinline__ int learned_rank(const uint16_t *mv, Move m) {
  * for an exclusive request on a busy node). */
 __device__ bool node_enter(Worker &W, Frame &f, int ply, int &value) {
   W.nodes++;
-  f.key = search_key(f.pos, f.stm);
+  f.key = search_key(f.pos, f.th);
   Move ttm = 0;
   int ts, td, tb;
   Move tm;
@@ -303,12 +308,18 @@ __global__ void __launch_bounds__(TPB) k_search_pure(const uint64_t *__restrict_
                                                      int N, int nworkers, int depth, TTEntry *tt, u64 tt_mask,
                                                      uint32_t *busy, u64 busy_mask, uint32_t *done, SearchOut *out,
                                                      unsigned long long budget, uint32_t *status, uint32_t *active,
-                                                     int max_per_pos, LearnArgs la) {
+                                                     int max_per_pos, LearnArgs la, int sparse) {
   __shared__ EvalTables sT;
   for (int i = threadIdx.x; i < (int)(sizeof(EvalTables) / 4); i += TPB)
     ((uint32_t *)&sT)[i] = ((const uint32_t *)&kEvalDev)[i];
   __syncthreads();
-  const long long t = (long long)blockIdx.x * TPB + threadIdx.x;
+  /* dense: one worker per thread; sparse: one worker per warp (lane 0),
+   * when every worker fits on the GPU with a warp of its own */
+  long long t = (long long)blockIdx.x * TPB + threadIdx.x;
+  if (sparse) {
+    if (threadIdx.x & 31) return;
+    t >>= 5;
+  }
   if (t >= (long long)N * nworkers) return;
   int p = (int)(t % N);
 
@@ -359,6 +370,7 @@ __global__ void __launch_bounds__(TPB) k_search_pure(const uint64_t *__restrict_
     F[0].pos.p2 = b[2];
     F[0].pos.p3 = b[3];
     F[0].pos.cr = b[4];
+    F[0].th = compute_hash(F[0].pos, stm[p] & 1);
     F[0].stm = stm[p] & 1;
     F[0].depth = depth;
     F[0].alpha = -kSearchInf - 1;
@@ -415,6 +427,7 @@ __global__ void __launch_bounds__(TPB) k_search_pure(const uint64_t *__restrict_
       } else {
         Frame &g = F[ply + 1];
         g.pos = c;
+        g.th = f.th ^ 1ULL ^ cr_keys(f.pos.cr) ^ cr_keys(c.cr) ^ piece_delta(m);
         g.stm = f.stm ^ 1;
         g.depth = f.depth - 1;
         g.alpha = -f.beta;
@@ -548,13 +561,21 @@ int search_pure_launch(const uint64_t *d_boards, const uint8_t *d_stm, int n, in
   ZCHECK(cudaMemsetAsync(c.s_done, 0, (size_t)2 * n * sizeof(uint32_t), s));
   ZCHECK(cudaMemsetAsync(c.s_busy, 0, c.s_busy_entries * sizeof(uint32_t), s));
   ZCHECK(cudaMemsetAsync(c.s_status, 0, sizeof(uint32_t), s));
-  const long long threads = (long long)n * workers;
+  const long long total = (long long)n * workers;
   const int tpb = 128;
+  static int resident_blocks = 0;
+  if (!resident_blocks) {
+    int per_sm = 0;
+    ZCHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_search_pure<128>, tpb, 0));
+    resident_blocks = (per_sm > 0 ? per_sm : 1) * c.sms;
+  }
+  const int sparse = total <= (long long)resident_blocks * (tpb / 32) ? 1 : 0;
+  const long long threads = sparse ? total * 32 : total;
   const unsigned long long budget = 1ull << 40;
   ZCHECK(cudaEventRecord(c.ev[1], s));
   k_search_pure<128><<<(unsigned)((threads + tpb - 1) / tpb), tpb, 0, s>>>(
       d_boards, d_stm, n, workers, depth, tt, entries - 1, c.s_busy, c.s_busy_entries - 1, c.s_done,
-      (SearchOut *)c.s_out, budget, c.s_status, c.s_done + n, c.s_helpers_cap, la);
+      (SearchOut *)c.s_out, budget, c.s_status, c.s_done + n, c.s_helpers_cap, la, sparse);
   ZCHECK(cudaGetLastError());
   ZCHECK(cudaEventRecord(c.ev[2], s));
   k_search_scatter<<<(n + 127) / 128, 128, 0, s>>>((const SearchOut *)c.s_out, n, d_scores, d_moves, d_nodes);
