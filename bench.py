@@ -401,8 +401,7 @@ def run_engine(args):
     boards, stm, _ = z.make_positions(w["seed"] + 0x1000003 * rank, n, w["min_plies"], w["max_plies"],
                                       w["min_pieces"], 0, 0)
     depth = args.depth or 8
-    workers = args.workers or 32
-    z.engine_set_helpers(args.helpers)  # finished positions' workers join unfinished ones
+    workers = args.workers or 16
     have_net = learn.load(z)
     cases = [0] + ([1] if have_net else [])
     z.engine_id(boards[:32], stm[:32], min(depth, 5), workers, 0)  # warm-up (buffers, code)
@@ -422,8 +421,7 @@ def run_engine(args):
         "warmup": 1, "ms_per_step": round(p["ms_total"], 2), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded random playouts)",
         "config": {"workload": f"engine: {n} playouts of 20-40 plies, >=20 pieces, iterative deepening 1..{depth}",
-                   "workers_per_position": workers, "helper_cap": args.helpers,
-                   "tt": "8 GB TT1 + 2 GB TT2, 1/n per position"},
+                   "workers_per_position": workers, "tt": "8 GB TT1 + 2 GB TT2, 1/n per position"},
         "nodes_per_s": round(p["nodes"] / (p["ms_total"] / 1e3), 1), "nodes": p["nodes"],
         "clocks": clocks.summary(),
         "roofline": _node_roofline(z, p["nodes"] / (p["ms_total"] / 1e3), "ops_per_engine_node", "k_engine"),

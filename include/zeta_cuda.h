@@ -89,7 +89,7 @@ int zeta_perft_batch_noalloc(const uint64_t *d_boards, const uint8_t *d_stm, con
  * threads_per_block: 64..1024, multiple of 32; blocks_per_sm: 0 = from
  * occupancy; min_tasks: split the tree until at least this many subtree
  * tasks exist (0 = 4 x resident threads); task_depth: remaining depth of a
- * subtree task, 1..4; use_graph: capture the launch sequence in a CUDA
+ * subtree task, 1..3; use_graph: capture the launch sequence in a CUDA
  * graph and replay it while the shapes stay the same. */
 typedef struct {
   int threads_per_block;
@@ -205,11 +205,6 @@ int zeta_engine_batch(const uint64_t *boards, const uint8_t *stm, int n, int dep
 int zeta_engine_id(const uint64_t *boards, const uint8_t *stm, int n, int depth, int workers, uint64_t max_nodes,
                    int ordering, int32_t *scores, uint32_t *bestmoves, uint64_t *nodes, uint8_t *depth_done,
                    float *ms_total, float *ms_search, float *ms_net);
-/* Batch throughput (no reference counterpart): in zeta_engine_id runs
- * without a node budget, workers whose position is done join unfinished
- * positions of the batch, up to this many workers per position (0, the
- * default: off; values <= workers: off). */
-int zeta_engine_set_helpers(int max_workers_per_position);
 
 /* ------------------------------------------------------------------ */
 /* The move-ordering network (no counterpart in the reference): 768

@@ -88,7 +88,6 @@ SIGNATURES = {
                                           ctypes.c_int, _u32p, _u64p]),
     "zeta_engine_batch": (ctypes.c_int, [_u64p, _u8p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_uint64,
                                          _i32p, _u32p, _u64p, _u32p]),
-    "zeta_engine_set_helpers": (ctypes.c_int, [ctypes.c_int]),
     "zeta_engine_id": (ctypes.c_int, [_u64p, _u8p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_uint64,
                                       ctypes.c_int, _i32p, _u32p, _u64p, _u8p, ctypes.POINTER(ctypes.c_float),
                                       ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]),
@@ -362,10 +361,6 @@ def engine_batch(boards, stm, depth: int, workers: int = 1, max_nodes: int = (1 
                                             _ptr(scores, _i32p), _ptr(moves, _u32p), _ptr(nodes, _u64p),
                                             _ptr(pvs, _u32p) if with_pv else None))
     return (scores, moves, nodes, pvs) if with_pv else (scores, moves, nodes)
-
-
-def engine_set_helpers(max_workers_per_position: int) -> None:
-    _check(load_library().zeta_engine_set_helpers(max_workers_per_position))
 
 
 def engine_id(boards, stm, depth: int, workers: int = 1, ordering: int = 0, max_nodes: int = 0):

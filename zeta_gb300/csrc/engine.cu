@@ -55,11 +55,8 @@ struct EngineState {
   uint8_t *stm = nullptr;
   uint8_t *active = nullptr;
   int *ply = nullptr;
-  unsigned long long *pnodes = nullptr; /* helpers: per-position node counts */
-  uint32_t *pactive = nullptr, *joined = nullptr;
   u64 *hist_in = nullptr;
   bool hist_in_alloc = false;
-  bool helped = false; /* the last launch counted nodes per position (pnodes) */
 };
 
 EngineState g_eng;
@@ -93,12 +90,6 @@ int engine_reserve(int n, int w) {
     cudaFree(e.stm);
     cudaFree(e.active);
     cudaFree(e.ply);
-    cudaFree(e.pnodes);
-    cudaFree(e.pactive);
-    cudaFree(e.joined);
-    ZCHECK(cudaMalloc(&e.pnodes, n * sizeof(unsigned long long)));
-    ZCHECK(cudaMalloc(&e.pactive, n * sizeof(uint32_t)));
-    ZCHECK(cudaMalloc(&e.joined, n * sizeof(uint32_t)));
     ZCHECK(cudaMalloc(&e.finito, n * sizeof(uint32_t)));
     ZCHECK(cudaMalloc(&e.pv, (size_t)n * kEPly * sizeof(uint32_t)));
     ZCHECK(cudaMalloc(&e.boards, (size_t)n * 7 * sizeof(uint64_t)));
@@ -154,9 +145,6 @@ void engine_free() {
   cudaFree(e.stm);
   cudaFree(e.active);
   cudaFree(e.ply);
-  cudaFree(e.pnodes);
-  cudaFree(e.pactive);
-  cudaFree(e.joined);
   cudaFree(e.hist_in);
   e = EngineState();
 }
@@ -199,18 +187,6 @@ int engine_launch(int n, int w, int depth, uint64_t max_nodes, bool with_hist, b
   a.finito = e.finito;
   a.pv = e.pv;
   a.status = e.status;
-  /* helpers only without a node budget: the budget is worker 0's count */
-  const bool helping = c.e_helpers_cap > w && n > 1 && max_nodes == ~0ULL;
-  if (helping) {
-    a.helper_cap = c.e_helpers_cap;
-    a.pnodes = e.pnodes;
-    a.pactive = e.pactive;
-    a.joined = e.joined;
-    ZCHECK(cudaMemsetAsync(e.pnodes, 0, n * sizeof(unsigned long long), c.stream));
-    ZCHECK(cudaMemsetAsync(e.pactive, 0, n * sizeof(uint32_t), c.stream));
-    ZCHECK(cudaMemsetAsync(e.joined, 0, n * sizeof(uint32_t), c.stream));
-  }
-  e.helped = helping;
   if (learned) {
     a.ocache = (OrderEntry *)c.s_ocache;
     a.ocache_mask = c.s_ocache_entries - 1;
@@ -271,24 +247,6 @@ int engine_stage(const uint64_t *boards, const uint8_t *stm, int n, int w, const
 
 EngineState &engine_state() { return g_eng; }
 
-/* nodes per position of the last launch: summed over the position's own
- * workers, or counted per position when helpers moved between positions */
-cudaError_t engine_position_nodes(int n, int workers, std::vector<uint64_t> &out) {
-  EngineState &e = g_eng;
-  out.assign(n, 0);
-  if (e.helped) {
-    std::vector<unsigned long long> pn(n);
-    cudaError_t r = cudaMemcpy(pn.data(), e.pnodes, n * sizeof(unsigned long long), cudaMemcpyDeviceToHost);
-    for (int i = 0; i < n; i++) out[i] = pn[i];
-    return r;
-  }
-  std::vector<unsigned long long> cnt((size_t)n * workers * 4);
-  cudaError_t r = cudaMemcpy(cnt.data(), e.cnt, cnt.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost);
-  for (int i = 0; i < n; i++)
-    for (int w = 0; w < workers; w++) out[i] += cnt[((size_t)w * n + i) * 4];
-  return r;
-}
-
 }  // namespace zeta
 
 using namespace zeta;
@@ -336,12 +294,14 @@ extern "C" int zeta_engine_batch(const uint64_t *boards, const uint8_t *stm, int
   EngineState &e = engine_state();
   std::vector<uint32_t> pv((size_t)n * kEPly);
   ZCHECK(cudaMemcpy(pv.data(), e.pv, pv.size() * sizeof(uint32_t), cudaMemcpyDeviceToHost));
-  std::vector<uint64_t> pn;
-  ZCHECK(engine_position_nodes(n, workers, pn));
+  std::vector<unsigned long long> cnt((size_t)n * workers * 4);
+  ZCHECK(cudaMemcpy(cnt.data(), e.cnt, cnt.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
   for (int i = 0; i < n; i++) {
     scores[i] = (int32_t)pv[(size_t)i * kEPly];
     bestmoves[i] = pv[(size_t)i * kEPly + 1];
-    nodes[i] = pn[i];
+    uint64_t s = 0;
+    for (int w = 0; w < workers; w++) s += cnt[((size_t)w * n + i) * 4];
+    nodes[i] = s;
   }
   if (pvs) memcpy(pvs, pv.data(), pv.size() * sizeof(uint32_t));
   return ZETA_OK;
@@ -402,11 +362,9 @@ extern "C" int zeta_engine_id(const uint64_t *boards, const uint8_t *stm, int n,
     t_search += ms;
     ZCHECK(cudaMemcpy(pv.data(), e.pv, pv.size() * sizeof(uint32_t), cudaMemcpyDeviceToHost));
     ZCHECK(cudaMemcpy(cnt.data(), e.cnt, cnt.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
-    std::vector<uint64_t> pn;
-    ZCHECK(engine_position_nodes(n, workers, pn));
     for (int i = 0; i < n; i++) {
       if (!active[i]) continue;
-      nodes[i] += pn[i];
+      for (int w = 0; w < workers; w++) nodes[i] += cnt[((size_t)w * n + i) * 4];
       const uint32_t *P = &pv[(size_t)i * kEPly];
       const bool stopped = cnt[(size_t)i * 4] >= budget;
       if (stopped || (P[1] & 0x3FFFFFFFu) == 0) {
@@ -444,13 +402,5 @@ extern "C" int zeta_engine_id(const uint64_t *boards, const uint8_t *stm, int n,
   if (ms_total) *ms_total = tot;
   if (ms_search) *ms_search = t_search;
   if (ms_net) *ms_net = t_net;
-  return ZETA_OK;
-}
-
-/* Helpers of the batched engine: workers whose position is done join
- * unfinished ones, up to this many workers per position (0 = off). */
-extern "C" int zeta_engine_set_helpers(int max_workers_per_position) {
-  if (max_workers_per_position < 0) return set_error(ZETA_ERR_ARG, "helper cap must be >= 0");
-  ctx().e_helpers_cap = max_workers_per_position;
   return ZETA_OK;
 }

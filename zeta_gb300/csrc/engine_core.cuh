@@ -136,11 +136,6 @@ struct EngineArgs {
   uint32_t *noreq;
   uint32_t oreq_cap;
   int learned_top;
-  /* helpers (batch throughput): off when null or helper_cap <= W */
-  int helper_cap;              /* most workers on one position */
-  unsigned long long *pnodes;  /* N: nodes per position, summed over its workers */
-  uint32_t *pactive;           /* N: workers inside each position */
-  uint32_t *joined;            /* N: helpers that joined each position */
 };
 
 /* the move-ordering score of the reference's picker (zeta.cl:2087-2124) */
@@ -331,10 +326,11 @@ __host__ __device__ __noinline__ int e_gen(const Pos &p, const NodeSets &ns, int
 __host__ __device__ __noinline__ int e_eval(const Pos &p, const EvalTables *T) { return eval_white(p, *T); }
 
 
-/* One search of position p by thread t as worker gid1 - 1 of that
- * position (gid1 is the ABDADA lock value, unique among p's workers). */
-__host__ __device__ __noinline__ void engine_job(const EngineArgs &a, long long t, int p, int gid1, const EvalTables &sT,
-                                    unsigned job) {
+/* One worker (thread t = w * N + p) of the full-engine search. */
+__host__ __device__ void engine_worker(const EngineArgs &a, long long t, const EvalTables &sT) {
+  const int p = (int)(t % a.N), w = (int)(t / a.N);
+  if (a.active && !a.active[p]) return;
+
   EFrame *F = a.frames + t * kEFrames;
   Move *MV = a.moves + t * (long long)kEFrames * kEMoves;
   u64 *H = a.hist + t * kGamePly;
@@ -345,12 +341,13 @@ __host__ __device__ __noinline__ void engine_job(const EngineArgs &a, long long 
   TT1E *tt1 = a.tt1_slice > 1 ? a.tt1 + (u64)p * a.tt1_slice : nullptr;
   TT2E *tt2 = a.tt2_slice > 1 ? a.tt2 + (u64)p * a.tt2_slice : nullptr;
   const u64 mask1 = a.tt1_slice - 1, mask2 = a.tt2_slice - 1;
+  const int gid1 = w + 1;
   const int D = a.depth;
   const int ply_init = a.ply_init ? a.ply_init[p] : 0;
   const int ttage = ply_init & 0x3F;
   const uint64_t *B = a.boards + (long long)p * 7;
   const int stm0 = a.stm[p] & 1;
-  uint32_t prn = 0x9E3779B9u ^ (uint32_t)(t * 0x85EBCA6Bu) ^ (job * 0xC2B2AE35u) ^ 1u;
+  uint32_t prn = 0x9E3779B9u ^ (uint32_t)(t * 0x85EBCA6Bu) ^ 1u;
 
   C[0] = C[1] = C[2] = C[3] = 0;
   for (int k = 0; k <= ply_init && k < kGamePly; k++)
@@ -640,7 +637,7 @@ __host__ __device__ __noinline__ void engine_job(const EngineArgs &a, long long 
         !(g->mode & (MD_NULL | MD_IID)) && g->depth >= 4)
       lmove = E_NULLMOVE;
     if (bresearch) lmove = g->mh;
-    if (lmove == 0 && (tt1 && !tt2) && gid1 > 1 && !(g->state & (ST_QS | ST_KIC | ST_EXT)) &&
+    if (lmove == 0 && (tt1 && !tt2) && w > 0 && !(g->state & (ST_QS | ST_KIC | ST_EXT)) &&
         !(g->mode & (MD_NULL | MD_LMR | MD_IID)) && g->depth > 0 && g->todo >= 1)
       brandomize = true; /* lazy SMP helpers without TT2 */
     const Move pm = F[sd - 1].mh;
@@ -759,72 +756,6 @@ __host__ __device__ __noinline__ void engine_job(const EngineArgs &a, long long 
       }
       if (bm == 0 || is_inf(bsc)) break;
     }
-  }
-}
-
-ZE uint32_t e_add(uint32_t *p, uint32_t v) {
-#if defined(__CUDA_ARCH__)
-  return atomicAdd(p, v);
-#else
-  const uint32_t o = *p;
-  *p += v;
-  return o;
-#endif
-}
-
-/* One worker (thread t = w * N + p) of the full-engine search: its own
- * position first; then, when helping is on (helper_cap > W), it joins
- * unfinished positions of the batch as one more worker each, up to
- * helper_cap workers per position, so the batch's largest trees end with
- * the most workers.  A helper starts with empty killer and counter moves
- * and a lock value above the position's own workers. */
-__host__ __device__ void engine_worker(const EngineArgs &a, long long t, const EvalTables &sT) {
-  int p = (int)(t % a.N);
-  const int w = (int)(t / a.N);
-  if (a.active && !a.active[p]) return;
-  const bool helping = a.helper_cap > a.W && a.pnodes && a.pactive && a.joined;
-  unsigned long long *C = a.cnt + t * 4;
-  if (helping) e_add(a.pactive + p, 1u);
-  engine_job(a, t, p, w + 1, sT, 0);
-  if (!helping) return;
-#if defined(__CUDA_ARCH__)
-  atomicAdd(a.pnodes + p, C[0]);
-  atomicSub(a.pactive + p, 1u);
-#else
-  a.pnodes[p] += C[0];
-  a.pactive[p] -= 1;
-#endif
-  Move *KIL = a.killers + t * kEPly;
-  Move *CM = a.cmoves + t * 4096;
-  for (unsigned job = 1; job < 4096; job++) {
-    const unsigned h = (unsigned)(t * 0x9E3779B1u) + job * 0x85EBCA6Bu;
-    int q = -1;
-    for (int k = 0; k < a.N; k++) {
-      const int c = (int)((h + (unsigned)k) % (unsigned)a.N);
-      if (a.active && !a.active[c]) continue;
-      if (((volatile const uint32_t *)a.finito)[c]) continue;
-      if (e_add(a.pactive + c, 1u) < (uint32_t)a.helper_cap) {
-        q = c;
-        break;
-      }
-#if defined(__CUDA_ARCH__)
-      atomicSub(a.pactive + c, 1u);
-#else
-      a.pactive[c] -= 1;
-#endif
-    }
-    if (q < 0) break;
-    for (int i = 0; i < kEPly; i++) KIL[i] = 0;
-    for (int i = 0; i < 4096; i++) CM[i] = 0;
-    const int gid1 = a.W + (int)e_add(a.joined + q, 1u) + 1;
-    engine_job(a, t, q, gid1, sT, job);
-#if defined(__CUDA_ARCH__)
-    atomicAdd(a.pnodes + q, C[0]);
-    atomicSub(a.pactive + q, 1u);
-#else
-    a.pnodes[q] += C[0];
-    a.pactive[q] -= 1;
-#endif
   }
 }
 
