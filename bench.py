@@ -401,7 +401,7 @@ def run_engine(args):
     boards, stm, _ = z.make_positions(w["seed"] + 0x1000003 * rank, n, w["min_plies"], w["max_plies"],
                                       w["min_pieces"], 0, 0)
     depth = args.depth or 8
-    workers = args.workers or 16
+    workers = args.workers or 32
     have_net = learn.load(z)
     cases = [0] + ([1] if have_net else [])
     z.engine_id(boards[:32], stm[:32], min(depth, 5), workers, 0)  # warm-up (buffers, code)

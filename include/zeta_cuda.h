@@ -89,7 +89,7 @@ int zeta_perft_batch_noalloc(const uint64_t *d_boards, const uint8_t *d_stm, con
  * threads_per_block: 64..1024, multiple of 32; blocks_per_sm: 0 = from
  * occupancy; min_tasks: split the tree until at least this many subtree
  * tasks exist (0 = 4 x resident threads); task_depth: remaining depth of a
- * subtree task, 1..3; use_graph: capture the launch sequence in a CUDA
+ * subtree task, 1..4; use_graph: capture the launch sequence in a CUDA
  * graph and replay it while the shapes stay the same. */
 typedef struct {
   int threads_per_block;
