@@ -332,13 +332,16 @@ def run_search(args):
     d_nd = torch.zeros(n, dtype=torch.int64, device=dev)
     stream = torch.cuda.Stream(dev)
     torch.cuda.set_stream(stream)
-    # (workers per position, helper cap): helpers let finished workers join
+    # (launch form, workers per position, helper cap): form 1 = dense (one
+    # worker per thread), 3 = warp-cooperative (one worker per warp, the
+    # lanes score the last ply); helpers let finished workers join
     # unfinished positions up to `cap` workers each (0 = no helping)
-    workers_list = ([(args.workers, args.helpers)] if args.workers else
-                    [(1, 16), (1, 32), (16, 48), (32, 96), (32, 128)])
+    workers_list = ([(args.form, args.workers, args.helpers)] if args.workers else
+                    [(1, 32, 96), (1, 32, 128), (3, 1, 2), (3, 1, 4), (3, 2, 4), (3, 2, 8)])
     results = {}
     ref_scores = None
-    for W, cap in workers_list:
+    for form, W, cap in workers_list:
+        z.search_set_launch_form(form)
         z.search_set_helpers(cap)
         for _ in range(1 if len(workers_list) > 1 else args.warmup):
             z.tt_clear()
@@ -361,11 +364,11 @@ def run_search(args):
         if ref_scores is None:
             ref_scores = sc
         if not np.array_equal(sc, ref_scores):
-            raise SystemExit(f"root scores changed with {W} workers")
-        key = f"{W}/{cap}"
+            raise SystemExit(f"root scores changed with form {form}, {W} workers")
+        key = f"{['auto', 'dense', 'sparse', 'warp'][form]}:{W}/{cap}"
         results[key] = {"positions_per_s": n / dt, "ms_per_step": dt * 1e3, "kernel_ms": sum(kms) / len(kms),
                         "nodes_per_s": nodes / steps / dt, "nodes_per_step": nodes // steps}
-        print(json.dumps({"workers/helper_cap": key, **results[key]}), file=sys.stderr, flush=True)
+        print(json.dumps({"form:workers/helper_cap": key, **results[key]}), file=sys.stderr, flush=True)
     best_w = max(results, key=lambda k: results[k]["positions_per_s"])
     r = results[best_w]
     if rank == 0:
@@ -375,12 +378,14 @@ def run_search(args):
             "warmup": args.warmup, "ms_per_step": round(r["ms_per_step"], 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded random playouts)",
             "config": {"workload": f"search_batch: {n} playouts of 20-40 plies, >=20 pieces, depth {depth}",
-                       "workers_per_position/helper_cap": best_w,
+                       "form:workers_per_position/helper_cap": best_w,
                        "tt": "1 GiB, 16-byte entries, cleared every step"},
             "nodes_per_s": round(r["nodes_per_s"], 1), "nodes_per_step": r["nodes_per_step"],
             "sweep": {str(k): round(v["positions_per_s"], 2) for k, v in results.items()},
-            "roofline": _node_roofline(z, r["nodes_per_s"], "ops_per_search_node", "k_search_pure"),
+            "roofline": _node_roofline(z, r["nodes_per_s"], "ops_per_search_node",
+                                       "k_search_warp" if best_w.startswith("warp") else "k_search_pure"),
         }), flush=True)
+    z.search_set_launch_form(0)
     z.release()
 
 
@@ -634,6 +639,8 @@ def main():
     ap.add_argument("--depth", type=int, default=0, help="search depth (search_batch; default 7)")
     ap.add_argument("--workers", type=int, default=0, help="ABDADA workers per position (0 = sweep)")
     ap.add_argument("--helpers", type=int, default=0, help="helper cap: max workers per position (0 = none)")
+    ap.add_argument("--form", type=int, default=0,
+                    help="search_batch launch form with --workers: 0 auto, 1 dense, 2 sparse, 3 warp-cooperative")
     ap.add_argument("--tt2-mb", type=int, default=0,
                     help="smp: ABDADA table size (0 = no TT2: helpers randomise their move order instead)")
     args = ap.parse_args()

@@ -160,6 +160,14 @@ int zeta_search_set_learned_order(int top, int quiet_only);
 /* Workers that finish their own position help unfinished ones, up to this
  * many workers per position (0, the default: no helping). */
 int zeta_search_set_helpers(int max_workers_per_position);
+/* Launch form of both search kernels (the pure search and the full
+ * engine): 0 automatic (the default), 1 dense -- 32 workers per warp,
+ * one per thread -- or 2 sparse -- one worker per warp, on lane 0, the
+ * other lanes exit at once.  Automatic takes the sparse form when every
+ * worker of the launch can have a resident warp of its own.  Results do
+ * not depend on the form; only the speed does.  No counterpart in the
+ * reference (one OpenCL work item per worker, zeta.cl:852). */
+int zeta_search_set_launch_form(int form);
 /* zero the transposition tables (as a new game does, src/xboard.c:159-199) */
 int zeta_tt_clear(void);
 /* device time of the last search kernel, ms */

@@ -43,3 +43,16 @@ def test_library_is_built_for_sm_103a_only():
     recipe, which passes a single -gencode)."""
     from zeta_gb300 import build
     assert build.ARCH == ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def test_setting_arguments_are_checked_on_the_host():
+    """Settings are validated before any device work: a bad launch form or
+    learned-ordering width is an argument error, a good one is accepted."""
+    import zeta_gb300 as z
+    for bad in (-1, 4):
+        with pytest.raises(z.ZetaError):
+            z.search_set_launch_form(bad)
+    for form in (1, 2, 3, 0):
+        z.search_set_launch_form(form)
+    with pytest.raises(z.ZetaError):
+        z.search_set_learned_order(0)

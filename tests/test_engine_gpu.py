@@ -160,3 +160,25 @@ def test_engine_learned_ordering_runs(zeta_device):
         assert (dd >= 1).all() and ms_n > 0
         for i in range(16):
             assert int(mv[i]) in ol.genmoves(boards[i], int(stm[i]))
+
+
+@pytest.mark.parametrize("form", [1, 2])
+def test_engine_launch_forms_match_reference(zeta_device, form):
+    """Dense and sparse launches of an 8-position batch with one worker
+    each: every position equals the reference's search exactly."""
+    _need_reference()
+    z = zeta_device
+    w = z.WORKLOADS["engine"]
+    boards, stm, _ = ol.make_positions(w["seed"] + 3, 8, min_plies=w["min_plies"], max_plies=w["max_plies"],
+                                       min_pieces=w["min_pieces"], min_depth=0, max_depth=0)
+    z.search_set_launch_form(form)
+    try:
+        z.tt_clear()
+        sc, mv, nodes, pvs = z.engine_batch(boards, stm, 5, 1, with_pv=True)
+    finally:
+        z.search_set_launch_form(0)
+    for i in range(8):
+        ref = ol.RefSearch(E1 // 8, E2 // 8)
+        pv_r, c_r = ref.run(boards[i], int(stm[i]), 5)
+        assert list(pvs[i]) == list(pv_r), (form, i)
+        assert sc[i] == np.int32(pv_r[0]) and mv[i] == pv_r[1] and nodes[i] == c_r[0, 1]

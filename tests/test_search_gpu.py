@@ -82,3 +82,63 @@ def test_benchmark_workload_depth7_is_worker_independent(zeta_device):
     b, _, _ = z.search_batch(boards, stm, 7, 8)
     c, _, _ = z.search_batch(boards, stm, 7, 8)
     assert np.array_equal(a, b) and np.array_equal(b, c)
+
+
+@pytest.mark.parametrize("form", [1, 2, 3])
+def test_launch_forms_give_the_same_scores(zeta_device, form):
+    """Dense (32 workers per warp), sparse (one per warp) and warp-cooperative
+    (one worker per warp whose lanes score the last ply together) launches
+    of the same batch: root scores equal the oracle's negamax in all."""
+    z = zeta_device
+    boards, stm, _ = _positions(0xF0A11 + form, 40, 10, 80)
+    want = [ol.alphabeta(boards[i], stm[i], 4)[0] for i in range(len(stm))]
+    z.search_set_launch_form(form)
+    try:
+        for workers in (1, 5):
+            z.tt_clear()
+            scores, moves, nodes = z.search_batch(boards, stm, 4, workers)
+            assert list(scores) == want, (form, workers)
+            assert (nodes > 0).all()
+    finally:
+        z.search_set_launch_form(0)
+
+
+def test_warp_form_depths_mates_best_moves_and_helpers(zeta_device):
+    """The warp-cooperative form at depths 1-5 (depth 1: the root itself
+    is scored by the lanes), with mated, stalemated and mate-in-one roots,
+    several workers and helpers: root scores equal negamax, and the best
+    move's child has the root's value."""
+    z = zeta_device
+    boards, stm, _ = _positions(0x3A4B, 24, 10, 90)
+    extra = [ol.setboard(f) for f in ("6k1/5ppp/8/8/8/8/5PPP/3R2K1 w - - 0 1",
+                                      "rnb1kbnr/pppp1ppp/8/4p3/6Pq/5P2/PPPPP2P/RNBQKBNR w KQkq - 1 3",
+                                      "7k/5Q2/6K1/8/8/8/8/8 b - - 0 1")]
+    boards = np.concatenate([boards, np.stack([b for b, _ in extra])])
+    stm = np.concatenate([stm, np.array([s for _, s in extra], np.uint8)])
+    z.search_set_launch_form(3)
+    try:
+        for depth in (1, 2, 3, 4, 5):
+            want = [ol.alphabeta(boards[i], stm[i], depth)[0] for i in range(len(stm))]
+            for workers, helpers in ((1, 0), (3, 0), (1, 4)):
+                z.search_set_helpers(helpers)
+                z.tt_clear()
+                scores, moves, nodes = z.search_batch(boards, stm, depth, workers)
+                assert list(scores) == want, (depth, workers, helpers)
+                assert (nodes > 0).all()
+            if depth <= 3:
+                for i in range(len(stm)):
+                    legal = ol.genmoves(boards[i], stm[i])
+                    if not legal:
+                        assert moves[i] == 0
+                        continue
+                    assert moves[i] in legal
+                    child = ol.play(boards[i], stm[i], int(moves[i]))
+                    v = ol.alphabeta(child, 1 - stm[i], depth - 1)[0] if depth > 1 else None
+                    if v is None:
+                        continue
+                    if abs(v) > 30000:
+                        v = v - 1 if v > 0 else v + 1
+                    assert -v == scores[i], (depth, i)
+    finally:
+        z.search_set_launch_form(0)
+        z.search_set_helpers(0)

@@ -115,6 +115,7 @@ SIGNATURES = {
     "zeta_search_set_learned_order": (ctypes.c_int, [ctypes.c_int, ctypes.c_int]),
     "zeta_tt_clear": (ctypes.c_int, []),
     "zeta_search_set_helpers": (ctypes.c_int, [ctypes.c_int]),
+    "zeta_search_set_launch_form": (ctypes.c_int, [ctypes.c_int]),
     "zeta_search_last_ms": (ctypes.c_int, [ctypes.POINTER(ctypes.c_float)]),
     "zeta_genmoves_batch": (ctypes.c_int, [_u64p, _u8p, ctypes.c_int, ctypes.c_int, _u32p, _i32p]),
 }
@@ -239,6 +240,11 @@ def search_batch_device(d_boards: int, d_stm: int, n: int, depth: int, workers: 
 
 def search_set_helpers(max_workers_per_position: int) -> None:
     _check(load_library().zeta_search_set_helpers(max_workers_per_position))
+
+
+def search_set_launch_form(form: int) -> None:
+    """Search kernels' launch form: 0 automatic, 1 dense (32 workers per warp), 2 sparse (one per warp)."""
+    _check(load_library().zeta_search_set_launch_form(form))
 
 
 def gemm_configure(ctas_per_sm: int) -> None:

@@ -357,6 +357,13 @@ int zeta_search_set_helpers(int max_workers_per_position) {
   return ZETA_OK;
 }
 
+int zeta_search_set_launch_form(int form) {
+  if (form < 0 || form > 3)
+    return set_error(ZETA_ERR_ARG, "launch form must be 0 (auto), 1 (dense), 2 (sparse) or 3 (warp)");
+  g_ctx.s_launch_form = form;
+  return ZETA_OK;
+}
+
 int zeta_tt_clear(void) {
   int rc = require_ready();
   if (rc) return rc;

@@ -108,6 +108,7 @@ struct Context {
   uint64_t s_busy_entries = 0;
   uint32_t *s_status = nullptr;
   int s_helpers_cap = 0;      /* max workers per position once helpers join; 0 = no helpers */
+  int s_launch_form = 0;      /* search kernels: 0 auto, 1 dense, 2 sparse */
   int s_learned_top = 12;     /* network moves used by the learned ordering */
   int s_learned_quiet = 1;    /* 1: they order the quiet moves only */
   void *s_ocache = nullptr;   /* learned ordering: OrderEntry cache */

@@ -206,7 +206,10 @@ int engine_launch(int n, int w, int depth, uint64_t max_nodes, bool with_hist, b
     ZCHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_engine<kEngineTPB>, kEngineTPB, 0));
     resident_blocks = (per_sm > 0 ? per_sm : 1) * c.sms;
   }
-  const int sparse = total <= (long long)resident_blocks * (kEngineTPB / 32) ? 1 : 0;
+  /* form 3 (warp-cooperative) is a pure-search form: the engine takes its automatic choice */
+  const int form = c.s_launch_form == 1 || c.s_launch_form == 2 ? c.s_launch_form : 0;
+  const int sparse = form ? (form == 2 ? 1 : 0)
+                          : (total <= (long long)resident_blocks * (kEngineTPB / 32) ? 1 : 0);
   const long long threads = sparse ? total * 32 : total;
   const int blocks = (int)((threads + kEngineTPB - 1) / kEngineTPB);
   ZCHECK(cudaEventRecord(c.ev[0], c.stream));

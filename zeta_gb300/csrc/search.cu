@@ -474,6 +474,314 @@ __global__ void __launch_bounds__(TPB) k_search_pure(const uint64_t *__restrict_
   }
 }
 
+/* Hand-off from a warp's tree walker (lane 0) to all 32 lanes: a node with
+ * one ply left and its legal moves, in shared memory. */
+struct LeafBatch {
+  Pos pos;
+  int n, ply, beta;
+  uint32_t stm;
+  Move moves[kMaxMoves];
+};
+
+/* Warp-cooperative form: one warp is one ABDADA worker.  Lane 0 walks the
+ * tree as k_search_pure does down to the nodes with one ply left; the
+ * children of such a node are then played and scored by all 32 lanes at
+ * once, 32 moves per round (lane i takes move r * 32 + i in round r), and
+ * a warp reduction after each round gives the best value so far.  A round
+ * whose best reaches the node's beta ends the node with that lower bound;
+ * a node whose moves were all scored has its exact value.  Either is
+ * stored in the table as such, so only the number of leaves visited
+ * changes and the root value is plain negamax as before.  The nodes with
+ * two or more plies left (move ordering, ABDADA, the table, killers, the
+ * learned ordering) are the k_search_pure walk unchanged. */
+template <int TPB>
+__global__ void __launch_bounds__(TPB) k_search_warp(const uint64_t *__restrict__ boards, const uint8_t *__restrict__ stm,
+                                                     int N, int nworkers, int depth, TTEntry *tt, u64 tt_mask,
+                                                     uint32_t *busy, u64 busy_mask, uint32_t *done, SearchOut *out,
+                                                     unsigned long long budget, uint32_t *status, uint32_t *active,
+                                                     int max_per_pos, LearnArgs la) {
+  __shared__ EvalTables sT;
+  __shared__ LeafBatch LB[TPB / 32];
+  for (int i = threadIdx.x; i < (int)(sizeof(EvalTables) / 4); i += TPB)
+    ((uint32_t *)&sT)[i] = ((const uint32_t *)&kEvalDev)[i];
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const long long t = ((long long)blockIdx.x * TPB + threadIdx.x) >> 5; /* worker = warp */
+  if (t >= (long long)N * nworkers) return;                              /* whole warps leave */
+  LeafBatch &B = LB[threadIdx.x >> 5];
+
+  Frame F[kMaxSearchDepth + 1]; /* lane 0's stack; the other lanes never touch theirs */
+  Worker W;
+  W.tt = tt;
+  W.tt_mask = tt_mask;
+  W.busy = busy;
+  W.busy_mask = busy_mask;
+  W.T = &sT;
+  W.learned = la.learned;
+  W.learned_top = la.top;
+  W.learned_quiet = la.quiet;
+  W.ocache = la.cache;
+  W.ocache_mask = la.mask;
+  W.oreq = la.req;
+  W.noreq = la.nreq;
+  W.oreq_cap = la.cap;
+  unsigned long long steps = 0;
+  int p = (int)(t % N), job = 0, ply = 0;
+  int phase = 0; /* lane 0: 0 take a job, 1 walk, 2 take a batch's value */
+  int pend = 0;  /* the batch is 1: the child F[ply + 1], 2: the root */
+  int bval = 0, bidx = 0, bdone = 0;
+
+  for (;;) {
+    int cmd = 0; /* 0: the worker stops; 1: score the batch in B */
+    if (lane == 0) {
+      for (;;) {
+        if (++steps > budget) {
+          atomicOr(status, SST_BUDGET);
+          break;
+        }
+        int val = 0;
+        bool deferred = false;
+        if (phase == 0) {
+          /* the worker's own position first, then unfinished ones, joining
+           * them as one more ABDADA worker from their root */
+          if (job > 0) {
+            if (max_per_pos <= nworkers) break; /* helping disabled */
+            const unsigned hsh = (unsigned)(t * 0x9E3779B1u + (unsigned)job * 0x85EBCA6Bu);
+            int q = -1;
+            for (int k = 0; k < N; k++) {
+              int c = (int)((hsh + (unsigned)k) % (unsigned)N);
+              if (((volatile uint32_t *)done)[c]) continue;
+              if (atomicAdd(&active[c], 1u) < (unsigned)max_per_pos) {
+                q = c;
+                break;
+              }
+              atomicSub(&active[c], 1u);
+            }
+            if (q < 0) break;
+            p = q;
+          } else {
+            atomicAdd(&active[p], 1u);
+          }
+          job++;
+          W.nodes = W.tthits = 0;
+          for (int i = 0; i <= kMaxSearchDepth; i++) W.killer[i][0] = W.killer[i][1] = 0;
+          const uint64_t *b = boards + 7 * (size_t)p;
+          F[0].pos.b0 = b[0];
+          F[0].pos.p1 = b[1];
+          F[0].pos.p2 = b[2];
+          F[0].pos.p3 = b[3];
+          F[0].pos.cr = b[4];
+          F[0].th = compute_hash(F[0].pos, stm[p] & 1);
+          F[0].stm = stm[p] & 1;
+          F[0].depth = depth;
+          F[0].alpha = -kSearchInf - 1;
+          F[0].beta = kSearchInf + 1;
+          F[0].exclusive = 0;
+          int v = 0;
+          bool open = false;
+          if (depth == 1) {
+            W.nodes++;
+            F[0].key = search_key(F[0].pos, F[0].th);
+            B.n = s_gen(F[0].pos, F[0].stm, B.moves);
+            if (B.n > 0) {
+              B.pos = F[0].pos;
+              B.stm = F[0].stm;
+              B.ply = 0;
+              B.beta = kSearchInf + 1;
+              pend = 2;
+              phase = 2;
+              cmd = 1;
+              break;
+            }
+            bool chk;
+            s_count(F[0].pos, F[0].stm, &chk);
+            v = chk ? -kSearchInf : 0;
+          } else {
+            open = node_enter(W, F[0], 0, v);
+          }
+          if (!open) {
+            /* no legal move at the root: the game is over */
+            if (atomicCAS(&done[p], 0u, 1u) == 0u) {
+              out[p].score = v;
+              out[p].bestmove = 0;
+            }
+            atomicAdd(&out[p].nodes, W.nodes);
+            atomicSub(&active[p], 1u);
+            continue;
+          }
+          ply = 0;
+          phase = 1;
+          continue;
+        }
+        if (phase == 2) {
+          /* the lanes scored every child of the batch node */
+          phase = 1;
+          W.nodes += bdone;
+          const Move bm = B.moves[bidx];
+          if (pend == 2) {
+            tt_store(W.tt, W.tt_mask, F[0].key, bval, 1, B_EXACT, bm);
+            if (atomicCAS(&done[p], 0u, 1u) == 0u) {
+              out[p].score = bval;
+              out[p].bestmove = bm;
+            }
+            atomicAdd(&out[p].nodes, W.nodes);
+            atomicAdd(&out[p].tthits, W.tthits);
+            atomicSub(&active[p], 1u);
+            phase = 0;
+            continue;
+          }
+          tt_store(W.tt, W.tt_mask, F[ply + 1].key, to_tt(bval, ply + 1), 1, bdone == B.n ? B_EXACT : B_LOWER,
+                   bm);
+          val = -bval;
+        } else {
+          if ((steps & 15) == 0 && ((volatile uint32_t *)done)[p]) {
+            /* another worker finished this position */
+            atomicAdd(&out[p].nodes, W.nodes);
+            atomicAdd(&out[p].tthits, W.tthits);
+            atomicSub(&active[p], 1u);
+            phase = 0;
+            continue;
+          }
+          Frame &f = F[ply];
+          while (f.i < f.n && ((f.moves[f.i] & kDone) || (f.iter == 1 && !(f.moves[f.i] & kDefer)))) f.i++;
+          if (f.i >= f.n) {
+            if (f.iter == 0 && f.deferred) {
+              f.iter = 1;
+              f.i = 0;
+              f.deferred = 0;
+              continue;
+            }
+            const int r = node_finish(W, f, ply);
+            if (ply == 0) {
+              if (atomicCAS(&done[p], 0u, 1u) == 0u) {
+                out[p].score = r;
+                out[p].bestmove = f.bestmove;
+              }
+              atomicAdd(&out[p].nodes, W.nodes);
+              atomicAdd(&out[p].tthits, W.tthits);
+              atomicSub(&active[p], 1u);
+              phase = 0;
+              continue;
+            }
+            ply--;
+            val = -r;
+          } else {
+            const Move m = f.moves[f.i] & kMoveBits;
+            Frame &g = F[ply + 1];
+            g.pos = f.pos;
+            play(g.pos, m, false);
+            g.th = f.th ^ 1ULL ^ cr_keys(f.pos.cr) ^ cr_keys(g.pos.cr) ^ piece_delta(m);
+            g.stm = f.stm ^ 1;
+            g.depth = f.depth - 1;
+            g.alpha = -f.beta;
+            g.beta = -(f.alpha > f.best ? f.alpha : f.best);
+            g.exclusive = (f.iter == 0 && f.searched > 0);
+            if (g.depth == 1) {
+              /* one ply left: a table hit, no legal move, or a batch */
+              W.nodes++;
+              g.key = search_key(g.pos, g.th);
+              int ts, td, tb;
+              Move tm;
+              bool hit = false;
+              if (tt_probe(W.tt, W.tt_mask, g.key, ts, td, tb, tm) && td == 1) {
+                const int s = from_tt(ts, ply + 1);
+                if (tb == B_EXACT || (tb == B_LOWER && s >= g.beta) || (tb == B_UPPER && s <= g.alpha)) {
+                  W.tthits++;
+                  val = -s;
+                  hit = true;
+                }
+              }
+              if (!hit) {
+                B.n = s_gen(g.pos, g.stm, B.moves);
+                if (B.n > 0) {
+                  B.pos = g.pos;
+                  B.stm = g.stm;
+                  B.ply = ply + 1;
+                  B.beta = g.beta;
+                  pend = 1;
+                  phase = 2;
+                  cmd = 1;
+                  break;
+                }
+                bool chk;
+                s_count(g.pos, g.stm, &chk);
+                val = chk ? kSearchInf - (ply + 1) : 0;
+              }
+            } else {
+              int cv;
+              if (node_enter(W, g, ply + 1, cv)) {
+                ply++;
+                continue;
+              }
+              if (cv == kOnEval) deferred = true;
+              else val = -cv;
+            }
+          }
+        }
+        /* a child of F[ply] returned `val` (or was deferred) */
+        Frame &h = F[ply];
+        if (deferred) {
+          h.moves[h.i] |= kDefer;
+          h.deferred = 1;
+          h.i++;
+          continue;
+        }
+        const Move m = h.moves[h.i] & kMoveBits;
+        h.moves[h.i] = m | kDone;
+        h.i++;
+        h.searched++;
+        if (val > h.best) {
+          h.best = val;
+          h.bestmove = m;
+        }
+        if (h.best > h.alpha) h.alpha = h.best;
+        if (h.best >= h.beta) {
+          if (!(m_pcpt(m) >> 1) && (m_pto(m) == m_pfrom(m)) && W.killer[ply][0] != m) {
+            W.killer[ply][1] = W.killer[ply][0];
+            W.killer[ply][0] = m;
+          }
+          h.i = h.n;
+          h.deferred = 0;
+        }
+      }
+    }
+    cmd = __shfl_sync(0xffffffffu, cmd, 0);
+    if (!cmd) break;
+    __syncwarp(); /* lane 0's batch is visible to the warp */
+    const int n = B.n, beta = B.beta;
+    int best = -kSearchInf - 1, bi = 0, scored = 0;
+    for (int base = 0; base < n; base += 32) {
+      const int i = base + lane;
+      if (i < n) {
+        Pos c = B.pos;
+        play(c, B.moves[i], false);
+        const int v = -leaf_value(c, B.stm ^ 1, B.ply + 1, &sT);
+        if (v > best) {
+          best = v;
+          bi = i;
+        }
+      }
+      /* the best value so far, the first move in generation order on ties;
+       * every lane ends with the same pair */
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const int ov = __shfl_xor_sync(0xffffffffu, best, o);
+        const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+        if (ov > best || (ov == best && oi < bi)) {
+          best = ov;
+          bi = oi;
+        }
+      }
+      scored = min(n, base + 32);
+      if (best >= beta) break; /* warp-uniform: the node fails high */
+    }
+    bval = best;
+    bidx = bi;
+    bdone = scored;
+    __syncwarp(); /* B is read by every lane before lane 0 writes it again */
+  }
+}
+
 __global__ void k_search_scatter(const SearchOut *out, int n, int32_t *scores, uint32_t *moves,
                                  unsigned long long *nodes) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -569,13 +877,20 @@ int search_pure_launch(const uint64_t *d_boards, const uint8_t *d_stm, int n, in
     ZCHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_search_pure<128>, tpb, 0));
     resident_blocks = (per_sm > 0 ? per_sm : 1) * c.sms;
   }
-  const int sparse = total <= (long long)resident_blocks * (tpb / 32) ? 1 : 0;
-  const long long threads = sparse ? total * 32 : total;
+  const int form = c.s_launch_form ? c.s_launch_form
+                                   : (total <= (long long)resident_blocks * (tpb / 32) ? 2 : 1);
+  const long long threads = form == 1 ? total : total * 32;
+  const unsigned blocks = (unsigned)((threads + tpb - 1) / tpb);
   const unsigned long long budget = 1ull << 40;
   ZCHECK(cudaEventRecord(c.ev[1], s));
-  k_search_pure<128><<<(unsigned)((threads + tpb - 1) / tpb), tpb, 0, s>>>(
-      d_boards, d_stm, n, workers, depth, tt, entries - 1, c.s_busy, c.s_busy_entries - 1, c.s_done,
-      (SearchOut *)c.s_out, budget, c.s_status, c.s_done + n, c.s_helpers_cap, la, sparse);
+  if (form == 3)
+    k_search_warp<128><<<blocks, tpb, 0, s>>>(d_boards, d_stm, n, workers, depth, tt, entries - 1, c.s_busy,
+                                              c.s_busy_entries - 1, c.s_done, (SearchOut *)c.s_out, budget,
+                                              c.s_status, c.s_done + n, c.s_helpers_cap, la);
+  else
+    k_search_pure<128><<<blocks, tpb, 0, s>>>(d_boards, d_stm, n, workers, depth, tt, entries - 1, c.s_busy,
+                                              c.s_busy_entries - 1, c.s_done, (SearchOut *)c.s_out, budget,
+                                              c.s_status, c.s_done + n, c.s_helpers_cap, la, form == 2);
   ZCHECK(cudaGetLastError());
   ZCHECK(cudaEventRecord(c.ev[2], s));
   k_search_scatter<<<(n + 127) / 128, 128, 0, s>>>((const SearchOut *)c.s_out, n, d_scores, d_moves, d_nodes);
