@@ -337,17 +337,18 @@ def run_search(args):
     # lanes score the last ply); helpers let finished workers join
     # unfinished positions up to `cap` workers each (0 = no helping)
     workers_list = ([(args.form, args.workers, args.helpers)] if args.workers else
-                    [(1, 32, 96), (1, 32, 128), (3, 1, 2), (3, 1, 4), (3, 2, 4), (3, 2, 8)])
+                    [(1, 32, 128), (3, 1, 16), (3, 2, 16), (3, 2, 32), (3, 2, 64), (3, 3, 32)])
     results = {}
     ref_scores = None
-    for form, W, cap in workers_list:
+    names = ["auto", "dense", "sparse", "warp"]
+
+    def measure(form, W, cap, warm, steps):
         z.search_set_launch_form(form)
         z.search_set_helpers(cap)
-        for _ in range(1 if len(workers_list) > 1 else args.warmup):
+        for _ in range(warm):
             z.tt_clear()
             z.search_batch_device(d_b.data_ptr(), d_s.data_ptr(), n, depth, W, d_sc.data_ptr(), d_mv.data_ptr(),
                                   d_nd.data_ptr(), stream.cuda_stream)
-        steps = 1 if len(workers_list) > 1 else args.steps
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         nodes = 0
@@ -361,19 +362,30 @@ def run_search(args):
         torch.cuda.synchronize()
         dt = (time.perf_counter() - t0) / steps
         sc = d_sc.cpu().numpy().copy()
+        nonlocal ref_scores
         if ref_scores is None:
             ref_scores = sc
         if not np.array_equal(sc, ref_scores):
             raise SystemExit(f"root scores changed with form {form}, {W} workers")
-        key = f"{['auto', 'dense', 'sparse', 'warp'][form]}:{W}/{cap}"
-        results[key] = {"positions_per_s": n / dt, "ms_per_step": dt * 1e3, "kernel_ms": sum(kms) / len(kms),
-                        "nodes_per_s": nodes / steps / dt, "nodes_per_step": nodes // steps}
+        return {"positions_per_s": n / dt, "ms_per_step": dt * 1e3, "kernel_ms": sum(kms) / len(kms),
+                "nodes_per_s": nodes / steps / dt, "nodes_per_step": nodes // steps}
+
+    # the sweep takes one step per setting; the best setting is then timed
+    # over --steps steps after --warmup warm-up steps
+    for form, W, cap in workers_list:
+        key = f"{names[form]}:{W}/{cap}"
+        single = len(workers_list) == 1
+        results[key] = measure(form, W, cap, args.warmup if single else 1, args.steps if single else 1)
         print(json.dumps({"form:workers/helper_cap": key, **results[key]}), file=sys.stderr, flush=True)
     best_w = max(results, key=lambda k: results[k]["positions_per_s"])
-    r = results[best_w]
+    if len(workers_list) > 1:
+        form, W, cap = workers_list[list(results).index(best_w)]
+        r = measure(form, W, cap, args.warmup, args.steps)
+    else:
+        r = results[best_w]
     if rank == 0:
         print(json.dumps({
-            "metric": "batched search positions/s (fixed depth 7, root score = plain negamax)",
+            "metric": f"batched search positions/s (fixed depth {depth}, root score = plain negamax)",
             "value": round(r["positions_per_s"], 2), "unit": "positions/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(r["ms_per_step"], 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded random playouts)",
@@ -381,7 +393,8 @@ def run_search(args):
                        "form:workers_per_position/helper_cap": best_w,
                        "tt": "1 GiB, 16-byte entries, cleared every step"},
             "nodes_per_s": round(r["nodes_per_s"], 1), "nodes_per_step": r["nodes_per_step"],
-            "sweep": {str(k): round(v["positions_per_s"], 2) for k, v in results.items()},
+            "kernel_ms": round(r["kernel_ms"], 3),
+            "sweep_single_step": {str(k): round(v["positions_per_s"], 2) for k, v in results.items()},
             "roofline": _node_roofline(z, r["nodes_per_s"], "ops_per_search_node",
                                        "k_search_warp" if best_w.startswith("warp") else "k_search_pure"),
         }), flush=True)

@@ -160,13 +160,17 @@ int zeta_search_set_learned_order(int top, int quiet_only);
 /* Workers that finish their own position help unfinished ones, up to this
  * many workers per position (0, the default: no helping). */
 int zeta_search_set_helpers(int max_workers_per_position);
-/* Launch form of both search kernels (the pure search and the full
- * engine): 0 automatic (the default), 1 dense -- 32 workers per warp,
- * one per thread -- or 2 sparse -- one worker per warp, on lane 0, the
- * other lanes exit at once.  Automatic takes the sparse form when every
- * worker of the launch can have a resident warp of its own.  Results do
- * not depend on the form; only the speed does.  No counterpart in the
- * reference (one OpenCL work item per worker, zeta.cl:852). */
+/* Launch form of the search kernels: 0 automatic (the default), 1 dense --
+ * 32 workers per warp, one per thread --, 2 sparse -- one worker per warp,
+ * on lane 0, the other lanes exit at once -- or 3 warp-cooperative (pure
+ * search only) -- one worker per warp whose lane 0 walks the tree and
+ * whose 32 lanes score the children of every node with one ply left.
+ * Automatic takes, when every worker of the launch can have a resident
+ * warp of its own, the warp-cooperative form for the pure search and the
+ * sparse form for the full engine, else the dense form; the full engine
+ * treats 3 as automatic.  Root scores do not depend on the form; speed
+ * and node counts do.  No counterpart in the reference (one OpenCL work
+ * group per worker, zeta.cl:852). */
 int zeta_search_set_launch_form(int form);
 /* zero the transposition tables (as a new game does, src/xboard.c:159-199) */
 int zeta_tt_clear(void);
@@ -262,8 +266,10 @@ int zeta_int_peak(double *tops);
 /* ------------------------------------------------------------------ */
 /* Move generation on the device (test and tooling entry): legal moves of
  * n positions, max 256 each, in the reference packing; counts[i] moves
- * for board i.  qs != 0 keeps captures only.  Host buffers. */
-int zeta_genmoves_batch(const uint64_t *boards, const uint8_t *stm, int n, int qs, uint32_t *moves,
+ * for board i.  flags bit 0 keeps captures only; bits 1-2 pick the device
+ * generator: 0 the perft generator, 1 the search kernels'.  Both give the
+ * same set; the order within a list differs.  Host buffers. */
+int zeta_genmoves_batch(const uint64_t *boards, const uint8_t *stm, int n, int flags, uint32_t *moves,
                         int32_t *counts);
 
 #ifdef __cplusplus

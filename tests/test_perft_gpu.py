@@ -130,13 +130,30 @@ def test_batch_workload_sample_vs_reference_sum_of_children(zeta_device):
         assert int(sub.sum()) == int(whole[i])
 
 
-def test_genmoves_matches_oracle(zeta_device):
+@pytest.mark.parametrize("generator", [0, 1])
+def test_genmoves_matches_oracle(zeta_device, generator):
+    """Each device generator (perft, search kernels) gives the oracle's
+    legal set, move for move in the reference packing."""
     z = zeta_device
     boards, stm, _ = ol.make_positions(0xD00D, 400, min_plies=1, max_plies=200)
+    special = [ol.setboard(f) for f in (
+        "r3k2r/p1ppqpb1/bn2pnp1/3PN3/1p2P3/2N2Q1p/PPPBBPPP/R3K2R w KQkq - 0 1",   # castles, pins
+        "8/2p5/3p4/KP5r/1R3p1k/8/4P1P1/8 w - - 0 1",                             # en passant, pins
+        "r3k2r/Pppp1ppp/1b3nbN/nP6/BBP1P3/q4N2/Pp1P2PP/R2Q1RK1 w kq - 0 1",      # promotions, checks
+        "rnbq1k1r/pp1Pbppp/2p5/8/2B5/8/PPP1NnPP/RNBQK2R w KQ - 1 8",             # promotion captures
+        "4k3/8/8/8/8/8/8/4K2R w K - 0 1",
+        "8/8/8/8/8/5k2/3p4/5K2 b - - 0 1",
+        "R6r/8/8/2K5/5k2/8/8/r6R w - - 0 1",                                     # rook pins
+        "3k4/3p4/8/K1P4r/8/8/8/8 b - - 0 1",                                     # double push, ep pin
+        "8/8/1k6/2b5/2pP4/8/5K2/8 b - d3 0 1",                                   # ep capture
+        "7k/5Q2/6K1/8/8/8/8/8 b - - 0 1",                                        # stalemate
+        "rnb1kbnr/pppp1ppp/8/4p3/6Pq/5P2/PPPPP2P/RNBQKBNR w KQkq - 1 3")]        # mate
+    boards = np.concatenate([boards, np.stack([b for b, _ in special])])
+    stm = np.concatenate([stm, np.array([s for _, s in special], np.uint8)])
     for qs in (False, True):
-        lists = z.genmoves_batch(boards, stm, qs=qs)
+        lists = z.genmoves_batch(boards, stm, qs=qs, generator=generator)
         for i in range(len(stm)):
-            assert sorted(lists[i].tolist()) == sorted(ol.genmoves(boards[i], stm[i], qs)), i
+            assert sorted(lists[i].tolist()) == sorted(ol.genmoves(boards[i], stm[i], qs)), (generator, qs, i)
 
 
 def test_device_positions_match_oracle_generator(zeta_device):

@@ -407,13 +407,14 @@ def int_peak_tops() -> float:
     return t.value
 
 
-def genmoves_batch(boards: np.ndarray, stm: np.ndarray, qs: bool = False):
+def genmoves_batch(boards: np.ndarray, stm: np.ndarray, qs: bool = False, generator: int = 0):
+    """Legal moves on the device; generator 0 the perft generator, 1 the search kernels'."""
     b = np.ascontiguousarray(boards, dtype=np.uint64).reshape(-1, 7)
     s = np.ascontiguousarray(stm, dtype=np.uint8)
     n = b.shape[0]
     moves = np.zeros((n, 256), dtype=np.uint32)
     counts = np.zeros(n, dtype=np.int32)
-    _check(load_library().zeta_genmoves_batch(_ptr(b, _u64p), _ptr(s, _u8p), n, int(qs), _ptr(moves, _u32p),
+    _check(load_library().zeta_genmoves_batch(_ptr(b, _u64p), _ptr(s, _u8p), n, int(qs) | (generator << 1), _ptr(moves, _u32p),
                                               _ptr(counts, _i32p)))
     return [moves[i, : counts[i]].copy() for i in range(n)]
 

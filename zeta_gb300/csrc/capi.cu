@@ -381,7 +381,8 @@ int zeta_search_last_ms(float *kernel_ms) {
   return ZETA_OK;
 }
 
-int zeta_genmoves_batch(const uint64_t *boards, const uint8_t *stm, int n, int qs, uint32_t *moves, int32_t *counts) {
+int zeta_genmoves_batch(const uint64_t *boards, const uint8_t *stm, int n, int flags, uint32_t *moves,
+                        int32_t *counts) {
   int rc = require_ready();
   if (rc) return rc;
   if (!boards || !stm || !moves || !counts || n <= 0) return set_error(ZETA_ERR_ARG, "bad arguments");
@@ -396,7 +397,7 @@ int zeta_genmoves_batch(const uint64_t *boards, const uint8_t *stm, int n, int q
   if (e == cudaSuccess) e = cudaMalloc(&dc, (size_t)n * 4);
   if (e == cudaSuccess) e = cudaMemcpyAsync(db, boards, (size_t)n * 56, cudaMemcpyHostToDevice, c.stream);
   if (e == cudaSuccess) e = cudaMemcpyAsync(ds, stm, n, cudaMemcpyHostToDevice, c.stream);
-  if (e == cudaSuccess) rc = genmoves_launch(db, ds, n, qs, dm, dc, c.stream);
+  if (e == cudaSuccess) rc = genmoves_launch(db, ds, n, flags, dm, dc, c.stream);
   if (e == cudaSuccess && rc == ZETA_OK) e = cudaMemcpy(moves, dm, (size_t)n * 256 * 4, cudaMemcpyDeviceToHost);
   if (e == cudaSuccess && rc == ZETA_OK) e = cudaMemcpy(counts, dc, (size_t)n * 4, cudaMemcpyDeviceToHost);
   cudaFree(db);

@@ -108,7 +108,7 @@ struct Context {
   uint64_t s_busy_entries = 0;
   uint32_t *s_status = nullptr;
   int s_helpers_cap = 0;      /* max workers per position once helpers join; 0 = no helpers */
-  int s_launch_form = 0;      /* search kernels: 0 auto, 1 dense, 2 sparse */
+  int s_launch_form = 0;      /* search kernels: 0 auto, 1 dense, 2 sparse, 3 warp (pure search) */
   int s_learned_top = 12;     /* network moves used by the learned ordering */
   int s_learned_quiet = 1;    /* 1: they order the quiet moves only */
   void *s_ocache = nullptr;   /* learned ordering: OrderEntry cache */
@@ -156,7 +156,7 @@ void mlp_free();
 /* engine.cu: the full-engine search */
 int engine_clear(cudaStream_t s);
 void engine_free();
-int genmoves_launch(const uint64_t *d_boards, const uint8_t *d_stm, int n, int qs, uint32_t *d_moves,
+int genmoves_launch(const uint64_t *d_boards, const uint8_t *d_stm, int n, int flags, uint32_t *d_moves,
                     int32_t *d_counts, cudaStream_t stream);
 
 }  // namespace zeta

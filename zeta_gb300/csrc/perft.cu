@@ -32,6 +32,7 @@
 #include <cstdio>
 
 #include "context.cuh"
+#include "movegen_fast.cuh"
 
 namespace zeta {
 
@@ -310,13 +311,21 @@ __global__ void __launch_bounds__(TPB, MINB) k_perft_ws(const Task *__restrict__
   }
 }
 
+/* one thread per position: gen 0 the perft generator (gen_legal), 1 the
+ * search engine's (gen_engine) */
 __global__ void k_genmoves(const uint64_t *__restrict__ boards, const uint8_t *__restrict__ stm, int n, int qs,
-                           uint32_t *__restrict__ moves, int32_t *__restrict__ counts) {
+                           int gen, uint32_t *__restrict__ moves, int32_t *__restrict__ counts) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   Move list[256];
   Pos p = load_pos(boards + 7 * (size_t)i);
-  int k = gen_legal(p, stm[i] & 1, qs != 0, list);
+  int k;
+  if (gen == 1) {
+    const Sets sets = make_sets(p, stm[i] & 1);
+    k = gen_engine(p, sets, enemy_attacks(sets, stm[i] & 1), stm[i] & 1, qs != 0, list);
+  } else {
+    k = gen_legal(p, stm[i] & 1, qs != 0, list);
+  }
   counts[i] = k;
   for (int j = 0; j < k; j++) moves[(size_t)i * 256 + j] = list[j];
 }
@@ -520,9 +529,11 @@ int perft_run(const uint64_t *d_boards, const uint8_t *d_stm, const uint8_t *d_d
   return ZETA_OK;
 }
 
-int genmoves_launch(const uint64_t *d_boards, const uint8_t *d_stm, int n, int qs, uint32_t *d_moves,
+int genmoves_launch(const uint64_t *d_boards, const uint8_t *d_stm, int n, int flags, uint32_t *d_moves,
                     int32_t *d_counts, cudaStream_t s) {
-  k_genmoves<<<(n + 127) / 128, 128, 0, s>>>(d_boards, d_stm, n, qs, d_moves, d_counts);
+  const int qs = flags & 1, gen = (flags >> 1) & 3;
+  if (gen > 1) return set_error(ZETA_ERR_ARG, "genmoves: unknown generator");
+  k_genmoves<<<(n + 127) / 128, 128, 0, s>>>(d_boards, d_stm, n, qs, gen, d_moves, d_counts);
   ZCHECK(cudaGetLastError());
   ZCHECK(cudaStreamSynchronize(s));
   return ZETA_OK;

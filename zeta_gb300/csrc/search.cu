@@ -483,6 +483,21 @@ struct LeafBatch {
   Move moves[kMaxMoves];
 };
 
+/* Captures and promotions to the front of a batch with more than one
+ * round of moves, so that the first round holds the moves most likely to
+ * reach beta (order among the others kept). */
+__device__ __forceinline__ void batch_captures_first(LeafBatch &B) {
+  if (B.n <= 32) return;
+  int k = 0;
+  for (int i = 0; i < B.n; i++) {
+    const Move mv = B.moves[i];
+    if ((m_pcpt(mv) >> 1) || m_pto(mv) != m_pfrom(mv)) {
+      B.moves[i] = B.moves[k];
+      B.moves[k++] = mv;
+    }
+  }
+}
+
 /* Warp-cooperative form: one warp is one ABDADA worker.  Lane 0 walks the
  * tree as k_search_pure does down to the nodes with one ply left; the
  * children of such a node are then played and scored by all 32 lanes at
@@ -495,7 +510,7 @@ struct LeafBatch {
  * two or more plies left (move ordering, ABDADA, the table, killers, the
  * learned ordering) are the k_search_pure walk unchanged. */
 template <int TPB>
-__global__ void __launch_bounds__(TPB) k_search_warp(const uint64_t *__restrict__ boards, const uint8_t *__restrict__ stm,
+__global__ void __launch_bounds__(TPB, 4) k_search_warp(const uint64_t *__restrict__ boards, const uint8_t *__restrict__ stm,
                                                      int N, int nworkers, int depth, TTEntry *tt, u64 tt_mask,
                                                      uint32_t *busy, u64 busy_mask, uint32_t *done, SearchOut *out,
                                                      unsigned long long budget, uint32_t *status, uint32_t *active,
@@ -694,6 +709,7 @@ __global__ void __launch_bounds__(TPB) k_search_warp(const uint64_t *__restrict_
               if (!hit) {
                 B.n = s_gen(g.pos, g.stm, B.moves);
                 if (B.n > 0) {
+                  batch_captures_first(B);
                   B.pos = g.pos;
                   B.stm = g.stm;
                   B.ply = ply + 1;
@@ -871,14 +887,17 @@ int search_pure_launch(const uint64_t *d_boards, const uint8_t *d_stm, int n, in
   ZCHECK(cudaMemsetAsync(c.s_status, 0, sizeof(uint32_t), s));
   const long long total = (long long)n * workers;
   const int tpb = 128;
+  /* automatic form: warp-cooperative when every worker can have a resident
+   * warp of its own (it is the sparse form's walk with the last ply scored
+   * by the whole warp), else dense */
   static int resident_blocks = 0;
   if (!resident_blocks) {
     int per_sm = 0;
-    ZCHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_search_pure<128>, tpb, 0));
+    ZCHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_search_warp<128>, tpb, 0));
     resident_blocks = (per_sm > 0 ? per_sm : 1) * c.sms;
   }
   const int form = c.s_launch_form ? c.s_launch_form
-                                   : (total <= (long long)resident_blocks * (tpb / 32) ? 2 : 1);
+                                   : (total <= (long long)resident_blocks * (tpb / 32) ? 3 : 1);
   const long long threads = form == 1 ? total : total * 32;
   const unsigned blocks = (unsigned)((threads + tpb - 1) / tpb);
   const unsigned long long budget = 1ull << 40;
