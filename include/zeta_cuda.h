@@ -271,6 +271,10 @@ int zeta_int_peak(double *tops);
  * same set; the order within a list differs.  Host buffers. */
 int zeta_genmoves_batch(const uint64_t *boards, const uint8_t *stm, int n, int flags, uint32_t *moves,
                         int32_t *counts);
+/* Static evaluation on the device (test and tooling entry): the reference
+ * evaluation of zeta.cl:1479-1544 before the side-to-move negation, in
+ * centipawns from white's view, of n boards.  Host buffers. */
+int zeta_eval_batch(const uint64_t *boards, int n, int32_t *scores);
 
 #ifdef __cplusplus
 }

@@ -142,3 +142,24 @@ def test_warp_form_depths_mates_best_moves_and_helpers(zeta_device):
     finally:
         z.search_set_launch_form(0)
         z.search_set_helpers(0)
+
+
+def test_device_evaluation_matches_oracle(zeta_device):
+    """The device evaluation (white's view) equals the oracle's restatement
+    of the reference evaluation on every board: playouts of all lengths,
+    the benchmark workload, and the special positions."""
+    z = zeta_device
+    boards, stm, _ = _positions(0xE7A1, 20000, 1, 200)
+    w = z.WORKLOADS["search_batch"]
+    wb, _, _ = z.make_positions(w["seed"], 2000, w["min_plies"], w["max_plies"], w["min_pieces"], 0, 0)
+    special = [ol.setboard(f)[0] for f in (
+        "rnbqkbnr/pppppppp/8/8/8/8/PPPPPPPP/RNBQKBNR w KQkq - 0 1",
+        "r3k2r/Pppp1ppp/1b3nbN/nP6/BBP1P3/q4N2/Pp1P2PP/R2Q1RK1 w kq - 0 1",
+        "8/2p5/3p4/KP5r/1R3p1k/8/4P1P1/8 w - - 0 1",
+        "4k3/8/8/8/8/8/8/4K2R w K - 0 1",
+        "2b1kb2/8/8/8/8/8/8/2B1KB2 w - - 0 1")]                  # both bishop pairs
+    allb = np.concatenate([boards, wb, np.stack(special)])
+    got = z.eval_batch(allb)
+    want = np.array([ol.eval_white(b) for b in allb])
+    bad = np.nonzero(got != want)[0]
+    assert len(bad) == 0, (len(bad), bad[:5].tolist(), got[bad[:5]].tolist(), want[bad[:5]].tolist())

@@ -118,6 +118,7 @@ SIGNATURES = {
     "zeta_search_set_launch_form": (ctypes.c_int, [ctypes.c_int]),
     "zeta_search_last_ms": (ctypes.c_int, [ctypes.POINTER(ctypes.c_float)]),
     "zeta_genmoves_batch": (ctypes.c_int, [_u64p, _u8p, ctypes.c_int, ctypes.c_int, _u32p, _i32p]),
+    "zeta_eval_batch": (ctypes.c_int, [_u64p, ctypes.c_int, _i32p]),
 }
 
 _lib: Optional[ctypes.CDLL] = None
@@ -417,6 +418,14 @@ def genmoves_batch(boards: np.ndarray, stm: np.ndarray, qs: bool = False, genera
     _check(load_library().zeta_genmoves_batch(_ptr(b, _u64p), _ptr(s, _u8p), n, int(qs) | (generator << 1), _ptr(moves, _u32p),
                                               _ptr(counts, _i32p)))
     return [moves[i, : counts[i]].copy() for i in range(n)]
+
+
+def eval_batch(boards: np.ndarray) -> np.ndarray:
+    """Static evaluation (white's view) of n boards on the device."""
+    b = np.ascontiguousarray(boards, dtype=np.uint64).reshape(-1, 7)
+    out = np.zeros(b.shape[0], dtype=np.int32)
+    _check(load_library().zeta_eval_batch(_ptr(b, _u64p), b.shape[0], _ptr(out, _i32p)))
+    return out
 
 
 # workload definitions of the benchmark configurations (seeded, synthetic)

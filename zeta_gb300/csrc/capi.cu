@@ -381,6 +381,24 @@ int zeta_search_last_ms(float *kernel_ms) {
   return ZETA_OK;
 }
 
+int zeta_eval_batch(const uint64_t *boards, int n, int32_t *scores) {
+  int rc = require_ready();
+  if (rc) return rc;
+  if (!boards || !scores || n <= 0) return set_error(ZETA_ERR_ARG, "bad arguments");
+  uint64_t *db = nullptr;
+  int32_t *dsc = nullptr;
+  Context &c = g_ctx;
+  cudaError_t e = cudaMalloc(&db, (size_t)n * 56);
+  if (e == cudaSuccess) e = cudaMalloc(&dsc, (size_t)n * 4);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(db, boards, (size_t)n * 56, cudaMemcpyHostToDevice, c.stream);
+  if (e == cudaSuccess) rc = eval_launch(db, n, dsc, c.stream);
+  if (e == cudaSuccess && rc == ZETA_OK) e = cudaMemcpy(scores, dsc, (size_t)n * 4, cudaMemcpyDeviceToHost);
+  cudaFree(db);
+  cudaFree(dsc);
+  if (e != cudaSuccess) return cuda_fail(e, "zeta_eval_batch");
+  return rc;
+}
+
 int zeta_genmoves_batch(const uint64_t *boards, const uint8_t *stm, int n, int flags, uint32_t *moves,
                         int32_t *counts) {
   int rc = require_ready();

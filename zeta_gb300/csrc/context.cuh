@@ -151,6 +151,7 @@ int mlp_fill_order_cache(const OrderRequest *req, uint32_t nreq, OrderEntry *cac
 bool mlp_ready_for_search();
 int learn_buffers();
 int search_tt_clear(cudaStream_t s);
+int eval_launch(const uint64_t *d_boards, int n, int32_t *d_scores, cudaStream_t s);
 /* mlp.cu */
 void mlp_free();
 /* engine.cu: the full-engine search */

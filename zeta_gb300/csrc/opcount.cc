@@ -222,7 +222,11 @@ int main(int argc, char **argv) {
           " \"ops_per_counted_node\": %.2f,\n \"ops_per_interior_node\": %.2f,\n"
           " \"search_sample\": {\"positions\": 16, \"depth\": 5, \"horizon_nodes\": %llu, \"ops_per_horizon_node\": %.2f, "
           "\"interior_nodes\": %llu, \"ops_per_interior_node\": %.2f},\n"
-          " \"ops_per_search_node\": %.2f,\n \"ops_per_engine_node\": %.2f\n}\n",
+          " \"ops_per_search_node\": %.2f,\n \"ops_per_engine_node\": %.2f,\n"
+          " \"search_rule\": \"search node = make + hash + (horizon: legal-move count + evaluation | interior: "
+          "generation), averaged over a plain alpha-beta walk to depth 5 of 16 search-workload positions; engine "
+          "node = make + in-check test + generation + evaluation + hash (move ordering and table work not "
+          "counted)\"\n}\n",
           a.count_nodes, (double)a.count_ops / a.count_nodes, a.gen_nodes, (double)a.gen_ops / a.gen_nodes,
           b.count_nodes, (double)b.count_ops / b.count_nodes, b.gen_nodes, (double)b.gen_ops / b.gen_nodes,
           (double)b.count_ops / b.count_nodes, (double)b.gen_ops / b.gen_nodes, st.leaves, s_leaf, st.interior, s_int,

@@ -798,6 +798,20 @@ __global__ void __launch_bounds__(TPB, 4) k_search_warp(const uint64_t *__restri
   }
 }
 
+/* the static evaluation (white's view) of n boards, for the parity test */
+__global__ void k_eval(const uint64_t *__restrict__ boards, int n, int32_t *__restrict__ scores) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint64_t *b = boards + 7 * (size_t)i;
+  Pos p;
+  p.b0 = b[0];
+  p.p1 = b[1];
+  p.p2 = b[2];
+  p.p3 = b[3];
+  p.cr = b[4];
+  scores[i] = eval_white(p, kEvalDev);
+}
+
 __global__ void k_search_scatter(const SearchOut *out, int n, int32_t *scores, uint32_t *moves,
                                  unsigned long long *nodes) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -834,6 +848,13 @@ static int search_buffers(int n) {
     ZCHECK(cudaMalloc(&c.s_tt, c.s_tt_entries * sizeof(TTEntry)));
     ZCHECK(cudaMemset(c.s_tt, 0, c.s_tt_entries * sizeof(TTEntry)));
   }
+  return ZETA_OK;
+}
+
+int eval_launch(const uint64_t *d_boards, int n, int32_t *d_scores, cudaStream_t s) {
+  k_eval<<<(n + 127) / 128, 128, 0, s>>>(d_boards, n, d_scores);
+  ZCHECK(cudaGetLastError());
+  ZCHECK(cudaStreamSynchronize(s));
   return ZETA_OK;
 }
 
