@@ -370,19 +370,20 @@ def run_search(args):
         return {"positions_per_s": n / dt, "ms_per_step": dt * 1e3, "kernel_ms": sum(kms) / len(kms),
                 "nodes_per_s": nodes / steps / dt, "nodes_per_step": nodes // steps}
 
-    # the sweep takes one step per setting; the best setting is then timed
-    # over --steps steps after --warmup warm-up steps
-    for form, W, cap in workers_list:
-        key = f"{names[form]}:{W}/{cap}"
-        single = len(workers_list) == 1
-        results[key] = measure(form, W, cap, args.warmup if single else 1, args.steps if single else 1)
-        print(json.dumps({"form:workers/helper_cap": key, **results[key]}), file=sys.stderr, flush=True)
-    best_w = max(results, key=lambda k: results[k]["positions_per_s"])
+    # the sweep takes one step per setting; the best setting (or the one
+    # given) is then timed over --steps steps after --warmup warm-up steps
     if len(workers_list) > 1:
+        for form, W, cap in workers_list:
+            key = f"{names[form]}:{W}/{cap}"
+            results[key] = measure(form, W, cap, 1, 1)
+            print(json.dumps({"form:workers/helper_cap": key, **results[key]}), file=sys.stderr, flush=True)
+        best_w = max(results, key=lambda k: results[k]["positions_per_s"])
         form, W, cap = workers_list[list(results).index(best_w)]
-        r = measure(form, W, cap, args.warmup, args.steps)
     else:
-        r = results[best_w]
+        form, W, cap = workers_list[0]
+        best_w = f"{names[form]}:{W}/{cap}"
+    with ClockSampler(local) as clocks:
+        r = measure(form, W, cap, args.warmup, args.steps)
     if rank == 0:
         print(json.dumps({
             "metric": f"batched search positions/s (fixed depth {depth}, root score = plain negamax)",
@@ -393,7 +394,7 @@ def run_search(args):
                        "form:workers_per_position/helper_cap": best_w,
                        "tt": "1 GiB, 16-byte entries, cleared every step"},
             "nodes_per_s": round(r["nodes_per_s"], 1), "nodes_per_step": r["nodes_per_step"],
-            "kernel_ms": round(r["kernel_ms"], 3),
+            "kernel_ms": round(r["kernel_ms"], 3), "clocks": clocks.summary(),
             "sweep_single_step": {str(k): round(v["positions_per_s"], 2) for k, v in results.items()},
             "roofline": _node_roofline(z, r["nodes_per_s"], "ops_per_search_node",
                                        "k_search_warp" if best_w.startswith("warp") else "k_search_pure"),

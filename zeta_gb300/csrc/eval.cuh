@@ -4,9 +4,8 @@
  * view; a white piece on sq reads sq^56), pawn structure (blocked -15,
  * diagonal support +10 each, -30 per own pawn further back on the file),
  * bishop pair +-25.  The reference sums one work-item per square; here the
- * piece terms are a loop over each piece type's squares and the pawn terms
- * are set-wise shifts and popcounts.  Result in centipawns from white's
- * view.
+ * piece terms are a loop over the occupied squares and the pawn terms are
+ * set-wise shifts and popcounts.  Result in centipawns from white's view.
  *
  * The tables are the reference's values (they define the score); device
  * code keeps a copy in shared memory (EvalTables) so that lanes reading
@@ -54,25 +53,16 @@ static const EvalTables kEvalHost = {ZETA_EVAL_PST, ZETA_EVAL_CONTROL, ZETA_EVAL
 static __constant__ EvalTables kEvalDev = {ZETA_EVAL_PST, ZETA_EVAL_CONTROL, ZETA_EVAL_VALUES};
 #endif
 
-/* sum over the pieces of one side of +10, material, PST and control, one
- * piece type at a time: the type planes give each type's squares, so no
- * square needs its piece looked up, and +10 plus material is a popcount
- * (type = p1 | p2 << 1 | p3 << 2: P 1, N 2, K 3, B 4, R 5, Q 6) */
+/* sum over the pieces of one side of +10, material, PST and control */
 ZHD int eval_pieces(const Pos &p, u64 side, bool black, const EvalTables &T) {
-  const u64 n1 = ~p.p1, n2 = ~p.p2, n3 = ~p.p3;
-  const u64 types[6] = {p.p1 & n2 & n3, n1 & p.p2 & n3, p.p1 & p.p2 & n3,
-                        n1 & n2 & p.p3, p.p1 & n2 & p.p3, n1 & p.p2 & p.p3};
   int s = 0;
-#pragma unroll
-  for (int t = 1; t <= 6; t++) {
-    u64 w = types[t - 1] & side;
-    s += popc(w) * (10 + T.value[t]);
-    while (w) {
-      const int sq = ctz(w);
-      w &= w - 1;
-      const int v = black ? sq : (sq ^ 56);
-      s += T.pst[t][v] + T.control[v];
-    }
+  u64 w = side;
+  while (w) {
+    int sq = ctz(w);
+    w &= w - 1;
+    int t = piece_at(p, sq) >> 1;
+    int v = black ? sq : (sq ^ 56);
+    s += 10 + T.value[t] + T.pst[t][v] + T.control[v];
   }
   return s;
 }
