@@ -469,7 +469,7 @@ def run_smp(args):
     torch.cuda.set_device(local)
     z.init(local, 2048, args.tt2_mb)
     depth = args.depth or 12
-    wlist = [args.workers] if args.workers else [64, 128, 256, 512, 1024]
+    wlist = [args.workers] if args.workers else [64, 128, 192, 256, 384, 512, 1024]
     b = z.STARTPOS
 
     def run(W):
@@ -488,10 +488,13 @@ def run_smp(args):
 
     rows = []
     with ClockSampler(local) as clocks:
-        for W in wlist:  # the worker sweep (benchsmp's table)
-            rows.append(run(W))
+        # the worker sweep (benchsmp's table); multi-worker searches vary run
+        # to run, so each count is run three times and ranked by its median
+        for W in wlist:
+            trio = sorted((run(W) for _ in range(3 if len(wlist) > 1 else 1)), key=lambda r: r["seconds"])
+            rows.append(dict(trio[len(trio) // 2], runs_s=[r["seconds"] for r in trio]))
             print(json.dumps(rows[-1]), file=sys.stderr, flush=True)
-        # multi-worker searches vary run to run: repeat the fastest count
+        # then the best count again, --steps runs, reported by their median
         w_best = min(rows, key=lambda r: r["seconds"])["workers"]
         reps = [run(w_best) for _ in range(max(1, args.steps))]
         for r in reps:

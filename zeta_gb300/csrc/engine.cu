@@ -199,21 +199,23 @@ int engine_launch(int n, int w, int depth, uint64_t max_nodes, bool with_hist, b
   ZCHECK(cudaMemsetAsync(e.pv, 0, (size_t)n * kEPly * sizeof(uint32_t), c.stream));
   ZCHECK(cudaMemsetAsync(e.status, 0, sizeof(uint32_t), c.stream));
   const long long total = (long long)n * w;
-  /* sparse when every worker can have a resident warp of its own */
-  static int resident_blocks = 0;
-  if (!resident_blocks) {
+  /* sparse when every worker can have a resident warp of its own; the
+   * sparse form launches one-warp blocks, so that the block scheduler
+   * spreads the workers over all SMs instead of packing four per SM */
+  static int resident_warps = 0;
+  if (!resident_warps) {
     int per_sm = 0;
-    ZCHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_engine<kEngineTPB>, kEngineTPB, 0));
-    resident_blocks = (per_sm > 0 ? per_sm : 1) * c.sms;
+    ZCHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_engine<32>, 32, 0));
+    resident_warps = (per_sm > 0 ? per_sm : 1) * c.sms;
   }
   /* form 3 (warp-cooperative) is a pure-search form: the engine takes its automatic choice */
   const int form = c.s_launch_form == 1 || c.s_launch_form == 2 ? c.s_launch_form : 0;
-  const int sparse = form ? (form == 2 ? 1 : 0)
-                          : (total <= (long long)resident_blocks * (kEngineTPB / 32) ? 1 : 0);
-  const long long threads = sparse ? total * 32 : total;
-  const int blocks = (int)((threads + kEngineTPB - 1) / kEngineTPB);
+  const int sparse = form ? (form == 2 ? 1 : 0) : (total <= (long long)resident_warps ? 1 : 0);
   ZCHECK(cudaEventRecord(c.ev[0], c.stream));
-  k_engine<kEngineTPB><<<blocks, kEngineTPB, 0, c.stream>>>(a, sparse);
+  if (sparse)
+    k_engine<32><<<(unsigned)total, 32, 0, c.stream>>>(a, 1);
+  else
+    k_engine<kEngineTPB><<<(unsigned)((total + kEngineTPB - 1) / kEngineTPB), kEngineTPB, 0, c.stream>>>(a, 0);
   ZCHECK(cudaGetLastError());
   ZCHECK(cudaEventRecord(c.ev[1], c.stream));
   ZCHECK(cudaStreamSynchronize(c.stream));
