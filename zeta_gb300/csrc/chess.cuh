@@ -364,6 +364,35 @@ ZHD int count_legal(const Pos &p, int stm) {
   return count_legal_ex(p, stm, in_check);
 }
 
+/* A quick sufficient test for "the side to move has a legal move": out of
+ * check, any move of a piece that is not pinned is legal, so a free
+ * knight, pawn or slider with a first step it may take proves one without
+ * the attack map.  True: a legal move exists.  False: undecided (in check,
+ * or only the king, pinned pieces, en passant or castling could move) --
+ * the exact count decides.  in_check is set either way. */
+ZHD bool has_free_move(const Pos &p, int stm, bool &in_check) {
+  const Sets s = make_sets(p, stm);
+  const Guard g = make_guard(s, stm);
+  in_check = g.checkers != 0;
+  if (in_check) return false;
+  const u64 free_ = s.us & ~g.pinned, open = ~s.us, empty = ~s.occ;
+  if (knight_attacks(s.knights & free_) & open) return true;
+  const u64 R = s.rq & free_, B = s.bq & free_;
+  const u64 rstep = (R << 8) | (R >> 8) | ((R << 1) & ZETA_NOTA) | ((R >> 1) & ZETA_NOTH);
+  const u64 bstep = ((B << 9) & ZETA_NOTA) | ((B << 7) & ZETA_NOTH) | ((B >> 7) & ZETA_NOTA) | ((B >> 9) & ZETA_NOTH);
+  if ((rstep | bstep) & open) return true;
+  const u64 P = s.pawns & free_;
+  const u64 push = stm ? (P >> 8) : (P << 8);
+  return ((push & empty) | (pawn_attacks(P, stm) & s.them)) != 0;
+}
+
+/* count_legal_ex(...) > 0, with the quick test first */
+ZHD bool has_legal_ex(const Pos &p, int stm, bool &in_check) {
+  if (has_free_move(p, stm, in_check)) return true;
+  bool chk;
+  return count_legal_ex(p, stm, chk) > 0;
+}
+
 /* ---------------- make ----------------
  * Pieces (domove, zetaperft.cl:464-552) and moved flags. */
 ZHD Move make_move(int from, int to, int cpt, int pfrom, int pto, int pcpt) {

@@ -87,8 +87,10 @@ static unsigned long long walk(const Pos &p, int stm, int depth, Tally &t, unsig
 }
 
 /* Search nodes: the per-node work of the fixed-depth search kernel --
- * make the move, hash the child; at the horizon count the legal moves
- * (mate / stalemate) and evaluate, elsewhere generate the moves.  Walked
+ * make the move, hash the child; at the horizon test for a legal move
+ * (mate / stalemate: the quick free-move test, then the count when it
+ * cannot decide, as the search kernels do) and evaluate, elsewhere
+ * generate the moves.  Walked
  * as plain alpha-beta (no table) so that the mix of horizon and interior
  * nodes is that of a searched tree.  The full engine's node also tests
  * for check, generates (captures only in quiescence) and evaluates at
@@ -102,7 +104,7 @@ static int sab(const Pos &p, int stm, int depth, int alpha, int beta, int ply, S
   (void)compute_hash(p, stm);
   if (depth == 0) {
     bool chk = false;
-    int n = count_legal_ex(p, stm, chk);
+    const bool n = has_legal_ex(p, stm, chk);
     int v = n ? (stm ? -eval_white(p, kEvalHost) : eval_white(p, kEvalHost)) : (chk ? -32000 + ply : 0);
     t.leaf_ops += Counter::ops - before + make_ops;
     t.leaves++;
@@ -223,7 +225,8 @@ int main(int argc, char **argv) {
           " \"search_sample\": {\"positions\": 16, \"depth\": 5, \"horizon_nodes\": %llu, \"ops_per_horizon_node\": %.2f, "
           "\"interior_nodes\": %llu, \"ops_per_interior_node\": %.2f},\n"
           " \"ops_per_search_node\": %.2f,\n \"ops_per_engine_node\": %.2f,\n"
-          " \"search_rule\": \"search node = make + hash + (horizon: legal-move count + evaluation | interior: "
+          " \"search_rule\": \"search node = make + hash + (horizon: legal-move test (free-move test, count "
+          "when undecided) + evaluation | interior: "
           "generation), averaged over a plain alpha-beta walk to depth 5 of 16 search-workload positions; engine "
           "node = make + in-check test + generation + evaluation + hash (move ordering and table work not "
           "counted)\"\n}\n",

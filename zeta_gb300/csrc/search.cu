@@ -148,11 +148,21 @@ __device__ __noinline__ int s_gen(Pos p, int stm, Move *list) {
   return gen_engine(p, s, enemy_attacks(s, stm), stm, false, list);
 }
 __device__ __noinline__ int s_eval(Pos p, const EvalTables *T) { return eval_white(p, *T); }
+/* whether the side to move has a legal move, and whether it is in check:
+ * the quick test, then the exact count when it cannot decide */
+__device__ __noinline__ bool s_has_move(Pos p, int stm, bool *chk) {
+  bool c;
+  if (has_free_move(p, stm, c)) {
+    *chk = c;
+    return true;
+  }
+  return s_count(p, stm, chk) > 0;
+}
 
 /* value of a node with no depth left, from the side to move */
 __device__ __forceinline__ int leaf_value(const Pos &p, int stm, int ply, const EvalTables *T) {
   bool chk;
-  if (s_count(p, stm, &chk) == 0) return chk ? -kSearchInf + ply : 0;
+  if (!s_has_move(p, stm, &chk)) return chk ? -kSearchInf + ply : 0;
   int e = s_eval(p, T);
   return stm ? -e : e;
 }
