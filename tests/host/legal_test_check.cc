@@ -1,0 +1,53 @@
+/*
+ * legal_test_check.cc -- host build of the device chess core (chess.cuh)
+ * for the CPU tests: walks full move trees and checks that the quick
+ * free-move test (has_free_move, used at pure-search leaves) never claims
+ * a legal move where the exact count (count_legal_ex) finds none, that
+ * has_legal_ex equals "count > 0", and that both report the same in-check
+ * flag.  Arguments: b0:p1:p2:p3:cr:stm:depth per root.  Prints one line
+ * per root; exit status 1 on any disagreement.
+ */
+#include <cstdio>
+#include <cstdlib>
+
+#include "../../zeta_gb300/csrc/chess.cuh"
+
+using namespace zeta;
+
+static unsigned long long g_nodes = 0, g_bad = 0, g_quick = 0;
+
+static void walk(const Pos &p, int stm, int depth) {
+  bool c1, c2, c3;
+  const int n = count_legal_ex(p, stm, c1);
+  const bool quick = has_free_move(p, stm, c2);
+  const bool has = has_legal_ex(p, stm, c3);
+  g_nodes++;
+  g_quick += quick;
+  if ((quick && n == 0) || has != (n > 0) || c1 != c2 || c1 != c3) {
+    if (g_bad < 5) printf("disagreement: count %d quick %d has %d check %d/%d/%d\n", n, quick, has, c1, c2, c3);
+    g_bad++;
+  }
+  if (depth == 0) return;
+  Move list[256];
+  const int k = gen_legal(p, stm, false, list);
+  for (int i = 0; i < k; i++) {
+    Pos q = p;
+    play(q, list[i], false);
+    walk(q, stm ^ 1, depth - 1);
+  }
+}
+
+int main(int argc, char **argv) {
+  for (int r = 1; r < argc; r++) {
+    unsigned long long v[7];
+    char *s = argv[r];
+    for (int i = 0; i < 7; i++) {
+      v[i] = strtoull(s, &s, 0);
+      if (*s == ':') s++;
+    }
+    const Pos p{v[0], v[1], v[2], v[3], v[4]};
+    walk(p, (int)v[5], (int)v[6]);
+    printf("root %d: %llu nodes, %llu decided by the quick test, %llu disagreements\n", r, g_nodes, g_quick, g_bad);
+  }
+  return g_bad != 0;
+}
