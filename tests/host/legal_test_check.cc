@@ -1,16 +1,27 @@
 /*
- * legal_test_check.cc -- host build of the device chess core (chess.cuh)
- * for the CPU tests: walks full move trees and checks that the quick
- * free-move test (has_free_move, used at pure-search leaves) never claims
- * a legal move where the exact count (count_legal_ex) finds none, that
- * has_legal_ex equals "count > 0", and that both report the same in-check
- * flag.  Arguments: b0:p1:p2:p3:cr:stm:depth per root.  Prints one line
- * per root; exit status 1 on any disagreement.
+ * legal_test_check.cc -- host build of the device chess core (chess.cuh,
+ * movegen_fast.cuh, tables.cuh) for the CPU tests.  Walks full move trees
+ * and checks at every node that
+ *   - the quick free-move test (has_free_move, used at pure-search leaves)
+ *     never claims a legal move where the exact count (count_legal_ex)
+ *     finds none, has_legal_ex equals "count > 0", and all three report
+ *     the same in-check flag;
+ *   - the search kernels' generator (gen_engine) gives the perft
+ *     generator's (gen_legal) move set, all moves and captures only;
+ *   - the incremental Zobrist update of the search kernels (parent hash ^
+ *     side toggle ^ castle / en-passant keys ^ piece_delta) equals hashing
+ *     every child from scratch (compute_hash).
+ * Arguments: b0:p1:p2:p3:cr:stm:depth per root.  Prints one line per
+ * root; exit status 1 on any disagreement.
  */
+#include <algorithm>
 #include <cstdio>
 #include <cstdlib>
 
+#define ZE static inline
 #include "../../zeta_gb300/csrc/chess.cuh"
+#include "../../zeta_gb300/csrc/movegen_fast.cuh"
+#include "../../zeta_gb300/csrc/tables.cuh"
 
 using namespace zeta;
 
@@ -27,12 +38,31 @@ static void walk(const Pos &p, int stm, int depth) {
     if (g_bad < 5) printf("disagreement: count %d quick %d has %d check %d/%d/%d\n", n, quick, has, c1, c2, c3);
     g_bad++;
   }
+  const Sets sets = make_sets(p, stm);
+  const u64 danger = enemy_attacks(sets, stm);
+  for (int qs = 0; qs < 2; qs++) {
+    Move a[256], b[256];
+    const int na = gen_legal(p, stm, qs != 0, a);
+    const int nb = gen_engine(p, sets, danger, stm, qs != 0, b);
+    std::sort(a, a + na);
+    std::sort(b, b + nb);
+    if (na != nb || !std::equal(a, a + na, b)) {
+      if (g_bad < 5) printf("generators differ (qs %d): %d vs %d moves\n", qs, na, nb);
+      g_bad++;
+    }
+  }
   if (depth == 0) return;
   Move list[256];
   const int k = gen_legal(p, stm, false, list);
+  const u64 th = compute_hash(p, stm);
   for (int i = 0; i < k; i++) {
     Pos q = p;
     play(q, list[i], false);
+    const u64 inc = th ^ 1ULL ^ cr_keys(p.cr) ^ cr_keys(q.cr) ^ piece_delta(list[i]);
+    if (inc != compute_hash(q, stm ^ 1)) {
+      if (g_bad < 5) printf("incremental hash differs after move %08x\n", list[i]);
+      g_bad++;
+    }
     walk(q, stm ^ 1, depth - 1);
   }
 }

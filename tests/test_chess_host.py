@@ -1,7 +1,9 @@
-"""The device chess core compiled for the host (g++, no GPU): the quick
-free-move test of the pure-search leaves agrees with the exact legal-move
-count on every node of full move trees from positions with castling, en
-passant, promotions, pins and checks."""
+"""The device chess core compiled for the host (g++, no GPU), on every node
+of full move trees from positions with castling, en passant, promotions,
+pins and checks: the quick free-move test of the pure-search leaves agrees
+with the exact legal-move count, the search kernels' generator gives the
+perft generator's moves, and the incremental Zobrist update equals hashing
+from scratch."""
 import os
 import shutil
 import subprocess
@@ -37,7 +39,7 @@ def _arg(board, stm, depth):
     return ":".join(str(int(x)) for x in board[:5]) + f":{int(stm)}:{depth}"
 
 
-def test_quick_legal_test_agrees_with_the_count(checker):
+def test_leaf_test_generators_and_incremental_hash_agree(checker):
     args = []
     for fen, depth in ROOTS:
         b, s = ol.setboard(fen)
