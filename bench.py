@@ -140,11 +140,29 @@ def measured_peaks():
     return {}
 
 
+def shard_seed(seed: int, rank: int) -> int:
+    """The seed of rank `rank`'s shard of a workload: ranks are replicas
+    that each take their own positions (weak scaling)."""
+    return seed + 0x1000003 * rank
+
+
+def reduce_over_ranks(seconds: float, units: float, device) -> tuple[float, float]:
+    """The job's timing across replicas: the slowest rank's seconds and the
+    units all ranks processed (an all-reduce on the host's process group;
+    the search path itself has no collective)."""
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(seconds)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    c = torch.tensor([float(units)], dtype=torch.float64, device=device)
+    dist.all_reduce(c)
+    return float(t.item()), float(c.item())
+
+
 def workload_arrays(z, rank: int, n: int = 0):
     w = dict(z.WORKLOADS[WORKLOAD])
-    seed = w["seed"] + 0x1000003 * rank  # each rank its own shard
-    return z.make_positions(seed, n or w["n"], w["min_plies"], w["max_plies"], w["min_pieces"], w["min_depth"],
-                            w["max_depth"])
+    return z.make_positions(shard_seed(w["seed"], rank), n or w["n"], w["min_plies"], w["max_plies"],
+                            w["min_pieces"], w["min_depth"], w["max_depth"])
 
 
 def run_ours(args):
@@ -208,12 +226,7 @@ def run_ours(args):
     total_s = sum(step_ms) / 1e3
     leaves_rank = int(ref_counts.sum()) * args.steps
     if world > 1:
-        t = torch.tensor([total_s], dtype=torch.float64, device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_s = float(t.item())
-        c = torch.tensor([leaves_rank], dtype=torch.float64, device=dev)
-        dist.all_reduce(c)
-        leaves_all = float(c.item())
+        total_s, leaves_all = reduce_over_ranks(total_s, leaves_rank, dev)
     else:
         leaves_all = float(leaves_rank)
     value = leaves_all / total_s
@@ -321,7 +334,7 @@ def run_search(args):
     z.init(local, 1024, 0)
     w = dict(z.WORKLOADS["search_batch"])
     n = args.n or w["n"]
-    boards, stm, _ = z.make_positions(w["seed"] + 0x1000003 * rank, n, w["min_plies"], w["max_plies"],
+    boards, stm, _ = z.make_positions(shard_seed(w["seed"], rank), n, w["min_plies"], w["max_plies"],
                                       w["min_pieces"], 0, 0)
     depth = args.depth or 7
     dev = torch.device("cuda", local)
@@ -417,7 +430,7 @@ def run_engine(args):
     z.init(local, 8192, 2048)
     w = dict(z.WORKLOADS["engine"])
     n = args.n or 256
-    boards, stm, _ = z.make_positions(w["seed"] + 0x1000003 * rank, n, w["min_plies"], w["max_plies"],
+    boards, stm, _ = z.make_positions(shard_seed(w["seed"], rank), n, w["min_plies"], w["max_plies"],
                                       w["min_pieces"], 0, 0)
     depth = args.depth or 8
     workers = args.workers or 32
