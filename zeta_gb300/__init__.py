@@ -244,7 +244,8 @@ def search_set_helpers(max_workers_per_position: int) -> None:
 
 
 def search_set_launch_form(form: int) -> None:
-    """Search kernels' launch form: 0 automatic, 1 dense (32 workers per warp), 2 sparse (one per warp)."""
+    """Search kernels' launch form: 0 automatic, 1 dense (32 workers per warp), 2 sparse (one per
+    warp), 3 warp-cooperative (pure search: one worker per warp, the lanes score the last ply)."""
     _check(load_library().zeta_search_set_launch_form(form))
 
 

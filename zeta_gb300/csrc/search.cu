@@ -11,10 +11,13 @@
  * only change how much of the tree is visited.
  *
  * Layout and parallelism
- *  - One thread is one search worker.  A batch of N positions runs with W
- *    workers each: thread t works on position t % N as worker t / N, so
- *    the 32 lanes of a warp search 32 different positions and the workers
- *    of one position sit in different warps (ABDADA across warps).
+ *  - A batch of N positions runs with W workers each; worker t works on
+ *    position t % N, so the workers of one position sit in different warps
+ *    (ABDADA across warps).  Three launch forms: dense (k_search_pure, one
+ *    worker per thread: 32 positions per warp), sparse (k_search_pure, one
+ *    worker per warp on lane 0) and warp-cooperative (k_search_warp, one
+ *    worker per warp whose 32 lanes score the children of every node with
+ *    one ply left).
  *  - Workers of a position share a 16-byte-entry transposition table in
  *    HBM (1 GiB by default, 2^26 entries, shared by the whole batch):
  *    {key ^ data, data}, data = move | score<<32 | depth<<48 | bound<<56,
