@@ -10,7 +10,11 @@
  *     generator's (gen_legal) move set, all moves and captures only;
  *   - the incremental Zobrist update of the search kernels (parent hash ^
  *     side toggle ^ castle / en-passant keys ^ piece_delta) equals hashing
- *     every child from scratch (compute_hash).
+ *     every child from scratch (compute_hash), and compute_hash equals the
+ *     oracle's zo_computehash;
+ *   - the device evaluation source (eval.cuh) equals the oracle's
+ *     zo_eval_white.
+ * Linked with the oracle (oracle/zeta_oracle.c) as the checker.
  * Arguments: b0:p1:p2:p3:cr:stm:depth per root.  Prints one line per
  * root; exit status 1 on any disagreement.
  */
@@ -19,7 +23,9 @@
 #include <cstdlib>
 
 #define ZE static inline
+#include "../../oracle/zeta_oracle.h"
 #include "../../zeta_gb300/csrc/chess.cuh"
+#include "../../zeta_gb300/csrc/eval.cuh"
 #include "../../zeta_gb300/csrc/movegen_fast.cuh"
 #include "../../zeta_gb300/csrc/tables.cuh"
 
@@ -36,6 +42,11 @@ static void walk(const Pos &p, int stm, int depth) {
   g_quick += quick;
   if ((quick && n == 0) || has != (n > 0) || c1 != c2 || c1 != c3) {
     if (g_bad < 5) printf("disagreement: count %d quick %d has %d check %d/%d/%d\n", n, quick, has, c1, c2, c3);
+    g_bad++;
+  }
+  const zo_u64 b7[7] = {p.b0, p.p1, p.p2, p.p3, p.cr, 0, 0};
+  if (eval_white(p, kEvalHost) != zo_eval_white(b7) || compute_hash(p, stm) != zo_computehash(b7, stm)) {
+    if (g_bad < 5) printf("evaluation or hash differs from the oracle's\n");
     g_bad++;
   }
   const Sets sets = make_sets(p, stm);

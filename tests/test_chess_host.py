@@ -2,8 +2,8 @@
 of full move trees from positions with castling, en passant, promotions,
 pins and checks: the quick free-move test of the pure-search leaves agrees
 with the exact legal-move count, the search kernels' generator gives the
-perft generator's moves, and the incremental Zobrist update equals hashing
-from scratch."""
+perft generator's moves, the incremental Zobrist update equals hashing from
+scratch, and the hash and the evaluation equal the oracle's."""
 import os
 import shutil
 import subprocess
@@ -13,6 +13,7 @@ import pytest
 import oracle_lib as ol
 
 HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
 
 ROOTS = [
     ("rnbqkbnr/pppppppp/8/8/8/8/PPPPPPPP/RNBQKBNR w KQkq - 0 1", 4),
@@ -30,7 +31,10 @@ def checker(tmp_path_factory):
     if shutil.which("g++") is None:
         pytest.skip("g++ not available")
     exe = str(tmp_path_factory.mktemp("host") / "legal_test_check")
-    subprocess.run(["g++", "-O2", "-std=c++17", "-o", exe, os.path.join(HERE, "host", "legal_test_check.cc")],
+    obj = exe + "_oracle.o"
+    subprocess.run(["gcc", "-O2", "-std=c11", "-c", "-o", obj, os.path.join(ROOT, "oracle", "zeta_oracle.c")],
+                   check=True)
+    subprocess.run(["g++", "-O2", "-std=c++17", "-o", exe, os.path.join(HERE, "host", "legal_test_check.cc"), obj],
                    check=True)
     return exe
 
