@@ -63,6 +63,36 @@ def test_host_board_layer_matches_oracle(harness):
         assert [int(x) for x in b2[:4]] == [int(x) for x in b[:4]] and s2 == stm
 
 
+MALFORMED = ["", "garbage", "8/8/8/8/8/8/8/8 w - - 0 1", "k7/8/8/8/8/8/8/7K w - e 0 1",
+             "k7/8/8/8/8/8/8/7K w - z9 0 1", "k7/8/8/8/8/8/8/7K w - e9 0 1",
+             "rnbqkbnr/pppppppp/99/8/8/8/PPPPPPPP/RNBQKBNR w KQkq - 0 1", "/" * 40 + " w",
+             "K" * 300 + " b", "kK" * 40, "k7/8/8/8/8/8/8/7K x QQQQQQQQQQQQQQQQQQQQ abcdefghijklmnop 99999999999 -1",
+             "8/8/8/8/8/8/8/8/8/8/8/8/k6K w - - 0 1", "x" * 2000]
+
+
+def test_host_board_layer_survives_malformed_fens(tmp_path):
+    """Malformed FEN lines (no kings, rank overflow, odd en-passant fields,
+    over-long fields and lines) under AddressSanitizer and
+    UndefinedBehaviorSanitizer: no invalid access, and a board without
+    exactly one king per side is refused."""
+    src = tmp_path / "h.c"
+    src.write_text(HARNESS)
+    exe = tmp_path / "h_san"
+    r = subprocess.run(["gcc", "-O1", "-g", "-std=gnu11", "-fsanitize=address,undefined", "-fno-sanitize-recover=all",
+                        "-I", HOST, "-o", str(exe), str(src), os.path.join(HOST, "board.c")], capture_output=True)
+    if r.returncode != 0:
+        pytest.skip("sanitizer runtime not available: " + r.stderr.decode(errors="replace")[-200:])
+    out = subprocess.run([str(exe)], input="\n".join(MALFORMED) + "\n", capture_output=True, text=True,
+                         timeout=60)
+    assert out.returncode == 0, out.stderr[-2000:]
+    for line in out.stdout.strip().splitlines():
+        f = line.split("|")[0].split()
+        kings = int(f[3], 16) & int(f[4], 16) & ~int(f[5], 16)
+        black = int(f[2], 16)
+        one_each = bin(kings & black).count("1") == 1 and bin(kings & ~black).count("1") == 1
+        assert int(f[0]) == int(one_each), line
+
+
 def test_zeta_binary_help_runs_without_gpu():
     if not os.path.exists(ZETA):
         pytest.skip("host binary not built")
