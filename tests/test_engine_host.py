@@ -82,11 +82,19 @@ def test_special_positions_match_reference(host_engine, fen, depth):
     _compare(host_engine, b, stm, depth)
 
 
-def test_workload_positions_match_reference(host_engine):
-    boards, stm, _ = ol.make_positions(0x5A17A0000000005, 3, min_plies=20, max_plies=40, min_pieces=20,
+@pytest.mark.parametrize("i", range(12))
+def test_workload_positions_match_reference(host_engine, i):
+    boards, stm, _ = ol.make_positions(0x5A17A0000000005, 12, min_plies=20, max_plies=40, min_pieces=20,
                                        min_depth=0, max_depth=0)
-    for i in range(3):
-        _compare(host_engine, boards[i], int(stm[i]), 4)
+    _compare(host_engine, boards[i], int(stm[i]), 5)
+
+
+@pytest.mark.parametrize("i", range(8))
+def test_playout_positions_match_reference(host_engine, i):
+    """Playouts of 1-150 plies: openings, middlegames and endgames."""
+    boards, stm, _ = ol.make_positions(0x77C1, 8, min_plies=1, max_plies=150, min_pieces=0, min_depth=0,
+                                       max_depth=0)
+    _compare(host_engine, boards[i], int(stm[i]), 5)
 
 
 def test_repetition_history_matches_reference(host_engine):
