@@ -78,10 +78,12 @@ int zeta_perft_batch_device(const uint64_t *d_boards, const uint8_t *d_stm, cons
  *    ZETA_ERR_NOALLOC.
  *  - The first call on a device looks up the array's device address (its
  *    host-side name is not a device address); make that first call before
- *    any stream capture.
+ *    any stream capture.  That one-time set-up is serialised between host
+ *    threads.
  *  - All calls share the one array: calls that overlap on the GPU (other
- *    streams, other host threads) race and give wrong counts.  The call
- *    synchronises `stream` before returning. */
+ *    streams, other host threads) race and give wrong counts.  Every call
+ *    copies a status word back and synchronises `stream` before it
+ *    returns. */
 int zeta_perft_batch_noalloc(const uint64_t *d_boards, const uint8_t *d_stm, const uint8_t *d_depth, int n,
                              uint64_t *d_leaves, void *stream);
 
@@ -190,7 +192,9 @@ int zeta_search_last_ms(float *kernel_ms);
  * between calls until zeta_tt_clear, as the reference's device buffers do.
  *
  * One launch: cl_run_alphabeta + cl_read_memory (src/clrun.c:675-974,
- * 1150-1266).  hash_history: MAXGAMEPLY (1024) hashes of the game, entry
+ * 1150-1266), depth 0..63; depth 0 is the reference host's start-up
+ * warm-up (src/zeta.c:695), a quiescence search of the root as the
+ * reference kernel runs it.  hash_history: MAXGAMEPLY (1024) hashes of the game, entry
  * ply_init = this position (NULL: the root hash only); max_nodes stops the
  * search when worker 0 has made more moves (the reference's COUNTERS[1]
  * test).  pv: PV[0] score, PV[1..63] moves, zero when the search was

@@ -72,6 +72,11 @@ int zo_negamax(const zo_u64 board[7], int stm, int depth, zo_move *bestmove, zo_
 /* Same value computed by full-window alpha-beta (no TT); equals zo_negamax. */
 int zo_alphabeta(const zo_u64 board[7], int stm, int depth, zo_move *bestmove, zo_u64 *nodes);
 
+/* The same alpha-beta value with moves reordered (iterative deepening
+ * 1..depth, previous best move first, MVV-LVA captures, killers): only the
+ * visited-node count differs.  *bestmove reaches the score. */
+int zo_alphabeta_ordered(const zo_u64 board[7], int stm, int depth, zo_move *bestmove, zo_u64 *nodes);
+
 /* Seeded random legal playout (splitmix64): plays `plies` moves from the
  * initial position, uniform over zo_genmoves order; returns 0 if the game
  * ended (no legal move) before that. */

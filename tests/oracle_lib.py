@@ -171,6 +171,14 @@ def alphabeta(board, stm: int, depth: int):
     return v, m.value, nodes.value
 
 
+def alphabeta_ordered(board, stm: int, depth: int):
+    """The alpha-beta value with reordered moves (same value, fewer nodes)."""
+    m = ctypes.c_uint32()
+    nodes = ctypes.c_uint64()
+    v = oracle().zo_alphabeta_ordered(_b7(board), int(stm), int(depth), ctypes.byref(m), ctypes.byref(nodes))
+    return v, m.value, nodes.value
+
+
 def make_position(seed: int, i: int, min_plies: int, max_plies: int, min_pieces: int, min_depth: int,
                   max_depth: int):
     b = _B7()

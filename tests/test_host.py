@@ -114,7 +114,8 @@ def test_zeta_go_prints_the_reference_search():
     search with the host's default tables (256 MB TT1, no TT2)."""
     if ol.reference() is None:
         pytest.skip("reference kernels (oracle/_ref) not built")
-    r = subprocess.run([ZETA], input="new\nsd 6\ngo\nquit\n", capture_output=True, text=True, timeout=600, cwd=ROOT)
+    r = subprocess.run([ZETA], input="new\nst 600\nsd 6\ngo\nquit\n", capture_output=True, text=True, timeout=600,
+                       cwd=ROOT)
     assert r.returncode == 0, r.stderr
     lines = [l.split() for l in r.stdout.splitlines() if l[:1].isdigit()]
     assert [int(f[0]) for f in lines] == [1, 2, 3, 4, 5, 6]
@@ -126,6 +127,36 @@ def test_zeta_go_prints_the_reference_search():
         total += int(cnt[0, 1])
         assert int(f[1]) == int(np.int32(pv[0])) and int(f[3]) == total
         assert f[4:] == [ol.move2can(int(m)) for m in pv[1:1 + int(f[0])] if m]
+
+
+@pytest.mark.gpu
+def test_zeta_st_one_second_moves_in_time(tmp_path):
+    """Time control (src/xboard.c:426-438, src/search.c:194-198): after
+    `st 1` the engine answers `go` with a legal move within about a second,
+    without a depth limit, from the default configuration (one worker)."""
+    import time
+    p = subprocess.Popen([ZETA], stdin=subprocess.PIPE, stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True,
+                         cwd=tmp_path, bufsize=1)
+    try:
+        p.stdin.write("xboard\nprotover 2\nnew\nst 1\nping 7\n")
+        p.stdin.flush()
+        while "pong 7" not in p.stdout.readline():
+            pass
+        t0 = time.perf_counter()
+        p.stdin.write("go\n")
+        p.stdin.flush()
+        line = p.stdout.readline()
+        while line and not line.startswith("move "):
+            line = p.stdout.readline()
+        dt = time.perf_counter() - t0
+        p.stdin.write("quit\n")
+        p.stdin.flush()
+    finally:
+        p.wait(timeout=60)
+    assert line.startswith("move "), line
+    assert dt < 1.5, f"st 1 took {dt:.2f} s"
+    b, s = ol.setboard("rnbqkbnr/pppppppp/8/8/8/8/PPPPPPPP/RNBQKBNR w KQkq - 0 1")
+    assert line.split()[1] in {ol.move2can(m) for m in ol.genmoves(b, s)}
 
 
 @pytest.mark.gpu

@@ -4,9 +4,12 @@
   of ``include/zeta_cuda.h``, compiled for sm_103a only.
 * ``zeta_gb300/_build/zeta`` -- the C host (xboard / perft / selftest
   commands) linked against that library.
-* ``oracle/_build/libzeta_oracle.so`` and, where the reference tree or its
-  preprocessed kernels are present, ``oracle/_ref/librefzeta.so``: the
-  test oracle (built here, never loaded by the product path).
+* ``oracle/_build/libzeta_oracle.so`` and, where the reference tree or the
+  files preprocessed from it are present, ``oracle/_ref/librefzeta.so`` and
+  ``oracle/_ref/zeta_refhost``: the test oracle and the reference's own
+  host linked against this boundary (built by ``oracle/Makefile``'s
+  ``auto`` target, which knows where the reference lives; never loaded by
+  the product path).
 
 Translation units compile in parallel; no cmake.
 """
@@ -24,7 +27,6 @@ CSRC = os.path.join(PKG, "csrc")
 HOST = os.path.join(PKG, "host")
 BUILD = os.path.join(PKG, "_build")
 ORACLE = os.path.join(ROOT, "oracle")
-REFERENCE_SRC = "/root/reference/src"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"] + ARCH
@@ -102,17 +104,15 @@ def build_host(verbose: bool = False) -> str | None:
 
 
 def build_oracle(verbose: bool = False) -> None:
-    """The oracle is test infrastructure: built so tests can load it."""
+    """The oracle is test infrastructure: built so tests can load it.  The
+    reference parts are optional (absent where neither the reference tree
+    nor the files preprocessed from it exist)."""
     _run(["make", "-s", "-C", ORACLE])
-    ref_ii = [os.path.join(ORACLE, "_ref", f) for f in ("kernel_perft.ii", "kernel_search.ii")]
     try:
-        if os.path.isdir(REFERENCE_SRC):
-            _run(["make", "-s", "-C", ORACLE, "ref", f"REF={REFERENCE_SRC}"])
-        elif all(os.path.exists(p) for p in ref_ii):
-            _run(["make", "-s", "-C", ORACLE, "ref-so"])
-    except RuntimeError as e:  # the reference build is optional
+        _run(["make", "-s", "-C", ORACLE, "auto"])
+    except RuntimeError as e:
         if verbose:
-            print("reference kernels not built:", e, file=sys.stderr)
+            print("reference parts not built:", e, file=sys.stderr)
 
 
 def build_opcount(out: str | None = None) -> str:

@@ -262,7 +262,9 @@ extern "C" int zeta_engine_search(const uint64_t board[7], int stm, int depth, i
   Context &c = ctx();
   if (!c.ready) return set_error(ZETA_ERR_STATE, "zeta_init has not been called");
   if (!board || !pv || !counters) return set_error(ZETA_ERR_ARG, "null pointer");
-  if (depth < 1 || depth >= kEPly) return set_error(ZETA_ERR_ARG, "depth %d out of range 1..%d", depth, kEPly - 1);
+  /* depth 0 is the reference host's start-up warm-up (src/zeta.c:695): a
+   * quiescence search of the root, as the reference kernel runs it */
+  if (depth < 0 || depth >= kEPly) return set_error(ZETA_ERR_ARG, "depth %d out of range 0..%d", depth, kEPly - 1);
   if (workers < 1 || workers > 65536) return set_error(ZETA_ERR_ARG, "workers %d out of range", workers);
   if (ply_init < 0 || ply_init >= kGamePly) return set_error(ZETA_ERR_ARG, "ply_init %d out of range", ply_init);
   uint8_t s = (uint8_t)(stm & 1);

@@ -30,6 +30,7 @@
  */
 #include <algorithm>
 #include <cstdio>
+#include <mutex>
 
 #include "context.cuh"
 #include "movegen_fast.cuh"
@@ -78,8 +79,12 @@ __global__ void k_roots(const uint64_t *__restrict__ boards, const uint8_t *__re
 __global__ void __launch_bounds__(128) k_split(int level, const Task *__restrict__ in, Task *__restrict__ out,
                                                Task *__restrict__ fin, uint32_t cap_lvl, uint32_t cap_fin,
                                                uint32_t min_tasks, int rmax, PerftCounters *pc) {
-  /* a level that overflowed its array counted past it (and flagged
-   * ST_CAPACITY): read only what was stored */
+  /* After an overflow (ST_CAPACITY, set by an earlier level) the call's
+   * result is void and the host reports it; stop here.  A level that
+   * overflowed holds an unwritten gap below its capacity (the reservation
+   * that crossed the end was dropped whole), so its slots must not be read
+   * as tasks. */
+  if (pc->status & ST_CAPACITY) return;
   const uint32_t n_in = min(pc->level_n[level], cap_lvl);
   const bool last = level == kMaxLevels - 1;
   Move list[256];
@@ -239,6 +244,10 @@ __global__ void __launch_bounds__(TPB, MINB) k_perft_ws(const Task *__restrict__
   __shared__ uint32_t s_task;
 
   const int tid = threadIdx.x;
+  /* a split level overflowed: the task set is incomplete and the host
+   * reports the call as failed; every block leaves at once (uniformly: only
+   * the split kernels set this bit) */
+  if (pc->status & ST_CAPACITY) return;
   const uint32_t n = min(pc->n_final, cap_fin); /* tasks beyond the array were not stored */
   const uint32_t B = gridDim.x;
   const int per_round = min(TPB, (int)(cap3 / kMaxChildren));
@@ -568,6 +577,9 @@ struct NoAllocScratch {
 static __device__ __align__(256) unsigned char g_noalloc_scratch[sizeof(NoAllocScratch)];
 
 constexpr int kNoAllocMaxDevices = 64;
+/* per-device set-up results, written and read under g_noalloc_mu so that
+ * a host thread never sees the address without the launch geometry */
+std::mutex g_noalloc_mu;
 NoAllocScratch *g_noalloc_ptr[kNoAllocMaxDevices] = {nullptr};
 int g_noalloc_sms[kNoAllocMaxDevices] = {0};
 int g_noalloc_blocks[kNoAllocMaxDevices] = {0};
@@ -587,20 +599,26 @@ extern "C" int zeta_perft_batch_noalloc(const uint64_t *d_boards, const uint8_t 
   if (dev < 0 || dev >= kNoAllocMaxDevices) return set_error(ZETA_ERR_ARG, "device %d out of range", dev);
   /* set-up, once per device, with that device current: the host-side name
    * of the array is not a device address, so look the address up */
-  if (!g_noalloc_ptr[dev]) {
-    void *p = nullptr;
-    ZCHECK(cudaGetSymbolAddress(&p, g_noalloc_scratch));
-    int sms = 0, bps = 0;
-    ZCHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    ZCHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_perft_ws<128, 1>, 128, 0));
-    int blocks = sms * (bps > 0 ? bps : 1);
-    if (blocks > kNoAllocMaxBlocks) blocks = kNoAllocMaxBlocks;
-    g_noalloc_sms[dev] = sms;
-    g_noalloc_blocks[dev] = blocks;
-    g_noalloc_ptr[dev] = (NoAllocScratch *)p;
+  NoAllocScratch *S = nullptr;
+  int blocks = 0, sms = 0;
+  {
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+      void *p = nullptr;
+      ZCHECK(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+      int nsm = 0, bps = 0;
+      ZCHECK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+      ZCHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_perft_ws<128, 1>, 128, 0));
+      int nb = nsm * (bps > 0 ? bps : 1);
+      if (nb > kNoAllocMaxBlocks) nb = kNoAllocMaxBlocks;
+      g_noalloc_sms[dev] = nsm;
+      g_noalloc_blocks[dev] = nb;
+      g_noalloc_ptr[dev] = (NoAllocScratch *)p;
+    }
+    S = g_noalloc_ptr[dev];
+    blocks = g_noalloc_blocks[dev];
+    sms = g_noalloc_sms[dev];
   }
-  NoAllocScratch *S = g_noalloc_ptr[dev];
-  const int blocks = g_noalloc_blocks[dev], sms = g_noalloc_sms[dev];
   cudaStream_t s = (cudaStream_t)stream;
   /* the array keeps the previous call's contents: clear what must start at zero */
   ZCHECK(cudaMemsetAsync(&S->pc, 0, sizeof(PerftCounters), s));

@@ -16,7 +16,7 @@ Bitboard BOARD[7];
 int STM = WHITE, SD = MAXPLY - 1, PLY = 0, GAMEPLY = 0;
 Bitboard HashHistory[MAXGAMEPLY];
 Move MoveHistory[MAXGAMEPLY];
-Bitboard GLOBAL_BOARD[7];
+Bitboard *GLOBAL_BOARD = NULL;
 uint64_t *COUNTERS = NULL;
 uint32_t *PV = NULL;
 uint64_t *GLOBAL_HASHHISTORY = NULL;
@@ -25,8 +25,9 @@ uint64_t threadsX = 1, threadsY = 1, totalWorkUnits = 1;
 uint64_t tt1_memory = 256, tt2_memory = 0;
 int64_t nodes_per_second = 1000000;
 uint64_t MaxNodes = 0;
-int device_id = 0;
-int search_mode = 1;
+int timemode = 0, MovesLeft = 1, MaxMoves = 1;
+double TimeInc = 0, TimeBase = 5 * 1000, TimeLeft = 5 * 1000, MaxTime = 5 * 1000;
+int32_t opencl_device_id = 0;
 uint64_t ABNODECOUNT = 0, TTHITS = 0, TTSCOREHITS = 0, IIDHITS = 0;
 FILE *LogFile = NULL;
 
@@ -48,7 +49,8 @@ bool read_config(const char *path) {
     sscanf(line, "nodes_per_second: %" SCNi64 ";", &nodes_per_second);
     sscanf(line, "tt1_memory: %" SCNu64 ";", &tt1_memory);
     sscanf(line, "tt2_memory: %" SCNu64 ";", &tt2_memory);
-    sscanf(line, "device_id: %d;", &device_id);
+    sscanf(line, "opencl_device_id: %d;", &opencl_device_id);
+    sscanf(line, "device_id: %d;", &opencl_device_id);
   }
   fclose(f);
   MaxNodes = (uint64_t)nodes_per_second;
@@ -58,18 +60,21 @@ bool read_config(const char *path) {
 }
 
 bool engine_alloc(void) {
+  GLOBAL_BOARD = calloc(7, sizeof(Bitboard));
   COUNTERS = calloc(totalWorkUnits * 64, sizeof(uint64_t));
   PV = calloc(MAXPLY, sizeof(uint32_t));
   GLOBAL_HASHHISTORY = calloc(totalWorkUnits * MAXGAMEPLY, sizeof(uint64_t));
   RNUMBERS = calloc(totalWorkUnits * 64, sizeof(uint32_t));
-  return COUNTERS && PV && GLOBAL_HASHHISTORY && RNUMBERS;
+  return GLOBAL_BOARD && COUNTERS && PV && GLOBAL_HASHHISTORY && RNUMBERS;
 }
 
 void engine_free(void) {
+  free(GLOBAL_BOARD);
   free(COUNTERS);
   free(PV);
   free(GLOBAL_HASHHISTORY);
   free(RNUMBERS);
+  GLOBAL_BOARD = NULL;
   COUNTERS = NULL;
   PV = NULL;
   GLOBAL_HASHHISTORY = NULL;
@@ -84,7 +89,7 @@ static void die(void) {
 
 void perft(Bitboard *board, int stm, int depth) {
   ABNODECOUNT = 0;
-  memcpy(GLOBAL_BOARD, board, sizeof GLOBAL_BOARD);
+  memcpy(GLOBAL_BOARD, board, 7 * sizeof(Bitboard));
   memset(COUNTERS, 0, totalWorkUnits * 64 * sizeof(uint64_t));
   for (uint64_t i = 0; i < totalWorkUnits; i++)
     memcpy(&GLOBAL_HASHHISTORY[i * MAXGAMEPLY], HashHistory, sizeof HashHistory);
@@ -102,7 +107,10 @@ void benchsmp(Bitboard *board, int stm, int depth, uint64_t max_workers) {
   double secs[kMaxRuns];
   uint64_t nps[kMaxRuns], workers[kMaxRuns];
   int runs = 0;
-  const uint64_t saved = totalWorkUnits;
+  const uint64_t saved = totalWorkUnits, saved_nodes = MaxNodes;
+  const double saved_time = MaxTime;
+  MaxNodes = 0; /* a depth-limited benchmark: no node or time budget */
+  MaxTime = 1e15;
   if (max_workers < 1) max_workers = 1;
   for (uint64_t w = 1; runs < kMaxRuns;) {
     printf("### doing inits for benchsmp depth %d: ###\n", depth);
@@ -132,6 +140,8 @@ void benchsmp(Bitboard *board, int stm, int depth, uint64_t max_workers) {
               ttd, rel);
   }
   totalWorkUnits = saved;
+  MaxNodes = saved_nodes;
+  MaxTime = saved_time;
   engine_free();
   if (!engine_alloc()) die();
   if (!cl_release_device() || !cl_init_device("alphabeta_gpu")) die();
@@ -177,34 +187,51 @@ int selftest(void) {
 }
 
 /* Iterative deepening, one launch per depth, the table kept between them
- * (src/search.c:77-198).  Prints "depth score time nodes pv" lines. */
+ * (src/search.c:35-223).  Prints "depth score time nodes pv" lines.
+ * Budgets, as the reference's loop (src/search.c:194-198): a launch stops
+ * when worker 0 has made MaxNodes / totalWorkUnits moves, and no deeper
+ * iteration starts once the nodes so far times the estimated branching
+ * factor (ESTEBF) exceed MaxNodes, or the time so far times ESTEBF exceeds
+ * MaxTime.  (The reference compares seconds with MaxTime's milliseconds
+ * there, which leaves only its node budget in force; both are in force
+ * here.)  Once a node rate has been measured, a launch's node budget is
+ * also capped at what that rate covers in the time left, so a fixed time
+ * per move (`st`) holds even when nodes_per_second is not calibrated. */
 Move rootsearch(Bitboard *board, int stm, int depth) {
   Move best = MOVENONE;
   int score = 0;
   double start = get_time_ms();
   ABNODECOUNT = TTHITS = TTSCOREHITS = IIDHITS = 0;
-  memcpy(GLOBAL_BOARD, board, sizeof GLOBAL_BOARD);
+  memcpy(GLOBAL_BOARD, board, 7 * sizeof(Bitboard));
   for (uint64_t i = 0; i < totalWorkUnits; i++) {
     memcpy(&GLOBAL_HASHHISTORY[i * MAXGAMEPLY], HashHistory, sizeof HashHistory);
     for (int j = 0; j < 64; j++) RNUMBERS[i * 64 + j] = (uint32_t)rand();
   }
-  /* node budget of a move (the reference derives it from the clock,
-   * src/xboard.c:193); 0 = no budget, for depth-limited searches */
+  /* 0 = no node budget, for depth-limited searches */
   const uint64_t max_nodes = MaxNodes ? MaxNodes : UINT64_MAX / ESTEBF;
   const uint64_t budget = max_nodes / totalWorkUnits;
+  const double max_time_s = MaxTime / 1000.0;
+  double el = 0.0;
   int idf = 1;
   do {
+    uint64_t launch_budget = budget;
+    if (idf > 1 && el > 0.005 && ABNODECOUNT > 0) {
+      const double per_worker_rate = (double)ABNODECOUNT / el / (double)totalWorkUnits;
+      const double left = max_time_s - el;
+      const double cap = left > 0 ? left * per_worker_rate : 1.0;
+      if (cap < (double)launch_budget) launch_budget = cap < 1.0 ? 1 : (uint64_t)cap;
+    }
     memset(COUNTERS, 0, totalWorkUnits * 64 * sizeof(uint64_t));
-    if (!cl_write_objects() || !cl_run_alphabeta(stm, idf, budget) || !cl_read_memory()) die();
+    if (!cl_write_objects() || !cl_run_alphabeta(stm, idf, launch_budget) || !cl_read_memory()) die();
     for (uint64_t i = 0; i < totalWorkUnits; i++) {
       ABNODECOUNT += COUNTERS[i * 64 + 1];
       TTHITS += COUNTERS[i * 64 + 3];
       TTSCOREHITS += COUNTERS[i * 64 + 4];
       IIDHITS += COUNTERS[i * 64 + 5];
     }
-    double el = (get_time_ms() - start) / 1000.0;
+    el = (get_time_ms() - start) / 1000.0;
     if (idf == 1 && JUSTMOVE(PV[1]) != MOVENONE) best = PV[1]; /* a move anyway */
-    if (COUNTERS[1] < budget) { /* not stopped by the node budget */
+    if (COUNTERS[1] < launch_budget) { /* not stopped by the node budget */
       if (JUSTMOVE(PV[1]) != MOVENONE) best = PV[1];
       score = ((int32_t)PV[0] == INF || (int32_t)PV[0] == -INF) ? 0 : (int32_t)PV[0];
       /* xboard mate scores, src/search.c:131-137 */
@@ -221,11 +248,14 @@ Move rootsearch(Bitboard *board, int stm, int depth) {
       printf("\n");
       if (LogFile) fprintf(LogFile, "\n");
       fflush(stdout);
+    } else if (launch_budget < budget) {
+      break; /* stopped by the clock */
     }
     /* mate in n: no deeper iteration can change it (src/search.c:180-191) */
     if (score >= MATESCORE && score < INF && idf >= INF - score) break;
     if (score <= -MATESCORE && score > -INF && idf >= INF + score) break;
     idf++;
-  } while (idf <= depth && ABNODECOUNT * ESTEBF <= max_nodes && ABNODECOUNT > 1 && idf < MAXPLY);
+  } while (idf <= depth && el * ESTEBF < max_time_s && ABNODECOUNT * ESTEBF <= max_nodes && ABNODECOUNT > 1 &&
+           idf < MAXPLY);
   return best;
 }

@@ -10,6 +10,7 @@
 #include <stdint.h>
 #include <stdio.h>
 
+#include "../../include/clrun.h"
 #include "board.h"
 
 /* engine state (src/zeta.h) */
@@ -21,25 +22,23 @@ extern int GAMEPLY;
 extern Bitboard HashHistory[MAXGAMEPLY];
 extern Move MoveHistory[MAXGAMEPLY];
 
-/* device-boundary staging (what cl_write_objects/cl_read_memory move) */
-extern Bitboard GLOBAL_BOARD[7];
-extern uint64_t *COUNTERS;       /* totalWorkUnits * 64 */
-extern uint32_t *PV;             /* MAXPLY: PV[0] score, PV[1..] moves */
-extern uint64_t *GLOBAL_HASHHISTORY;
+/* device-boundary staging (what cl_write_objects/cl_read_memory move):
+ * GLOBAL_BOARD, COUNTERS, PV, GLOBAL_HASHHISTORY and the configuration
+ * globals are declared by include/clrun.h with the reference's types */
 extern uint32_t *RNUMBERS;
 
 /* configuration (config.txt keys, src/io.c:533-583) */
-extern uint64_t threadsX, threadsY, totalWorkUnits;
-extern uint64_t tt1_memory, tt2_memory;
-extern int64_t nodes_per_second;
 extern uint64_t MaxNodes;
-extern int device_id;
-extern int search_mode;          /* 1 the reference's search (default), 0 pure fixed-depth */
+
+/* time control (src/zeta.c:78-85): timemode 0 = fixed time per move
+ * (`st`), 1 = conventional clock (`level` with moves per session), 2 =
+ * incremental clock (`level 0 ...`); times in milliseconds */
+extern int timemode, MovesLeft, MaxMoves;
+extern double TimeInc, TimeBase, TimeLeft, MaxTime;
 
 /* results */
 extern uint64_t ABNODECOUNT, TTHITS, TTSCOREHITS, IIDHITS;
 
-extern FILE *LogFile;
 
 bool read_config(const char *path);
 bool engine_alloc(void);

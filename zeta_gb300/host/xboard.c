@@ -35,7 +35,16 @@ static void play_move(Move m) {
   }
 }
 
+/* the node budget of a move from its time (src/xboard.c:193, 371) */
+static void set_max_nodes(void) { MaxNodes = (uint64_t)(MaxTime / 1000 * (double)nodes_per_second); }
+
+/* moves left in this session (one move kept as spare), src/xboard.c:358-359 */
+static void update_moves_left(void) {
+  if (timemode == 1 && MaxMoves > 0) MovesLeft = (MaxMoves - (((PLY + 1) / 2) % MaxMoves)) + 1;
+}
+
 static void think_and_move(void) {
+  const double t0 = get_time_ms();
   Move m = rootsearch(BOARD, STM, SD);
   if (JUSTMOVE(m) == MOVENONE) {
     printf("resign\n");
@@ -46,6 +55,14 @@ static void think_and_move(void) {
   play_move(m);
   printf("move %s\n", mv);
   fflush(stdout);
+  /* clock after the move, src/xboard.c:355-371 */
+  TimeLeft -= get_time_ms() - t0;
+  update_moves_left();
+  if (timemode == 0) TimeLeft = TimeBase;
+  if (timemode == 2) TimeLeft += TimeInc;
+  MaxTime = TimeLeft / (MovesLeft > 0 ? MovesLeft : 1) + TimeInc;
+  if (timemode == 1 && MovesLeft == 2) TimeLeft += TimeBase;
+  set_max_nodes();
 }
 
 void xboard(void) {
@@ -67,6 +84,7 @@ void xboard(void) {
       new_game();
       force_mode = false;
       SD = MAXPLY - 1;
+      set_max_nodes();
     } else if (!strcmp(cmd, "setboard")) {
       int full;
       if (!board_setfen(BOARD, &STM, &full, arg)) printf("tellusererror Illegal position\n");
@@ -87,6 +105,43 @@ void xboard(void) {
       SD = atoi(arg);
       if (SD < 1) SD = 1;
       if (SD >= MAXPLY) SD = MAXPLY - 1;
+    } else if (!strcmp(cmd, "level")) {
+      /* level MPS BASE INC, BASE in minutes or min:sec (src/xboard.c:384-424) */
+      int mps = 0, min = 0, sec = 0;
+      double inc = 0;
+      if (sscanf(arg, "%d %d:%d %lf", &mps, &min, &sec, &inc) != 4 &&
+          sscanf(arg, "%d %d %lf", &mps, &min, &inc) != 3)
+        continue;
+      if (strchr(arg, ':') == NULL) sec = 0;
+      MaxMoves = mps;
+      TimeBase = (60.0 * min + sec) * 1000;
+      TimeInc = inc * 1000;
+      TimeLeft = TimeBase;
+      timemode = MaxMoves == 0 ? 2 : 1;
+      MovesLeft = timemode == 2 ? 40 : 1;
+      update_moves_left();
+      MaxTime = TimeLeft / MovesLeft + TimeInc;
+      set_max_nodes();
+    } else if (!strcmp(cmd, "st")) {
+      /* st SECONDS: a fixed time per move (src/xboard.c:426-438) */
+      double secs = 0;
+      if (sscanf(arg, "%lf", &secs) != 1 || secs <= 0) continue;
+      TimeBase = TimeLeft = secs * 1000;
+      TimeInc = 0;
+      MovesLeft = MaxMoves = 1;
+      timemode = 0;
+      MaxTime = TimeLeft / MovesLeft + TimeInc;
+      set_max_nodes();
+    } else if (!strcmp(cmd, "time")) {
+      /* time CENTISECONDS left on the engine's clock (src/xboard.c:440-453) */
+      double cs = 0;
+      if (sscanf(arg, "%lf", &cs) != 1) continue;
+      TimeLeft = cs * 10;
+      update_moves_left();
+      MaxTime = TimeLeft / (MovesLeft > 0 ? MovesLeft : 1) + TimeInc;
+      set_max_nodes();
+    } else if (!strcmp(cmd, "otim")) {
+      /* the opponent's clock: not used (src/xboard.c:455-456) */
     } else if (!strcmp(cmd, "ping")) {
       printf("pong %s", arg);
     } else if (!strcmp(cmd, "post")) {
@@ -117,10 +172,10 @@ void xboard(void) {
       board_getfen(BOARD, STM, 1 + PLY / 2, fen, sizeof fen);
       printf("# %s\n", fen);
     } else if (!strcmp(cmd, "help") && !xboard_mode) {
-      printf("# commands: new, setboard <fen>, go, usermove <move>, force, sd <depth>, perft <depth>,\n"
+      printf("# commands: new, setboard <fen>, go, usermove <move>, force, sd <depth>, st <seconds>,\n"
+             "# level <moves> <minutes> <increment>, time <centiseconds>, perft <depth>,\n"
              "# benchsmp [max workers], selftest, print, quit (and the xboard protocol)\n");
-    } else if (!strcmp(cmd, "accepted") || !strcmp(cmd, "rejected") || !strcmp(cmd, "level") ||
-               !strcmp(cmd, "st") || !strcmp(cmd, "time") || !strcmp(cmd, "otim") || !strcmp(cmd, "random") ||
+    } else if (!strcmp(cmd, "accepted") || !strcmp(cmd, "rejected") || !strcmp(cmd, "random") ||
                !strcmp(cmd, "computer") || !strcmp(cmd, "result") || !strcmp(cmd, "hard") ||
                !strcmp(cmd, "easy") || !strcmp(cmd, "name") || !strcmp(cmd, "rating") || !strcmp(cmd, "white") ||
                !strcmp(cmd, "black") || !strcmp(cmd, "draw") || !strcmp(cmd, "memory")) {
