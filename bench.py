@@ -285,8 +285,178 @@ def run_ours(args):
         "clocks": clocks.summary(),
         "device": {"sms": info["sms"], "cc": list(info["cc"]), "hbm_gbs_measured": peaks.get("hbm_gbs")},
     }
+    if not args.no_search:
+        z.release()
+        line["search_batch"] = search_batch_block(z, local, rank, args)
+        line["learned_ab"] = learned_ab_block(z, local, rank, args)
     print(json.dumps(line), flush=True)
     z.release()
+
+
+# The batched-search setting of the default line: the warp-cooperative form
+# with 2 ABDADA workers per position and finished workers helping the
+# unfinished positions up to 64 workers each (the fastest setting of the
+# --workload search_batch sweep).
+SEARCH_FORM, SEARCH_WORKERS, SEARCH_HELPERS = 3, 2, 64
+
+
+def _search_arrays(z, rank, n):
+    w = dict(z.WORKLOADS["search_batch"])
+    return z.make_positions(shard_seed(w["seed"], rank), n or w["n"], w["min_plies"], w["max_plies"],
+                            w["min_pieces"], 0, 0)[:2]
+
+
+def oracle_search_sample(boards, stm, depth: int, budget_s: float = 15.0):
+    """The oracle's plain alpha-beta (oracle/zeta_oracle.c, ordered moves,
+    the same root values) on the host cores, a bounded sample of the
+    workload: positions/s, labelled as the oracle, not the reference (the
+    reference has no pure fixed-depth search)."""
+    from concurrent.futures import ThreadPoolExecutor
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib as ol
+    cores = os.cpu_count() or 1
+    k = min(len(stm), cores)
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(cores) as ex:  # the ctypes calls release the GIL
+        vals = list(ex.map(lambda i: ol.alphabeta_ordered(boards[i], int(stm[i]), depth)[0], range(k)))
+    dt = time.perf_counter() - t0
+    if dt < budget_s / 4 and 2 * k <= len(stm):
+        k2 = min(len(stm), int(k * min(8.0, budget_s / max(dt, 1e-3))))
+        t0 = time.perf_counter()
+        with ThreadPoolExecutor(cores) as ex:
+            vals = list(ex.map(lambda i: ol.alphabeta_ordered(boards[i], int(stm[i]), depth)[0], range(k2)))
+        dt, k = time.perf_counter() - t0, k2
+    return {"value": round(k / dt, 3), "unit": "positions/s", "cores": cores, "kind": "port",
+            "label": "oracle, not reference",
+            "sample": f"oracle plain alpha-beta (ordered moves, no table) on {cores} host threads, first {k} "
+                      f"workload positions at depth {depth} in {dt:.1f}s"}, vals
+
+
+def search_batch_block(z, local, rank, args):
+    """Batched pure search (1024 playout positions, depth 7, 1 GiB table
+    cleared every step), device buffers, CUDA events on the launching
+    stream; root scores checked against the oracle on the CPU sample."""
+    import torch
+    z.init(local, 1024, 0)
+    boards, stm = _search_arrays(z, rank, 0)
+    n, depth = len(stm), 7
+    dev = torch.device("cuda", local)
+    d_b = torch.from_numpy(boards.view(np.int64)).to(dev)
+    d_s = torch.from_numpy(stm).to(dev)
+    d_sc = torch.zeros(n, dtype=torch.int32, device=dev)
+    d_mv = torch.zeros(n, dtype=torch.int32, device=dev)
+    d_nd = torch.zeros(n, dtype=torch.int64, device=dev)
+    stream = torch.cuda.Stream(dev)
+    z.search_set_launch_form(SEARCH_FORM)
+    z.search_set_helpers(SEARCH_HELPERS)
+
+    def step():
+        z.tt_clear()
+        z.search_batch_device(d_b.data_ptr(), d_s.data_ptr(), n, depth, SEARCH_WORKERS, d_sc.data_ptr(),
+                              d_mv.data_ptr(), d_nd.data_ptr(), stream.cuda_stream)
+
+    for _ in range(3):
+        step()
+    torch.cuda.synchronize()
+    steps = 3
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    kms, nodes = [], 0
+    with ClockSampler(local) as clocks:
+        for a, b in ev:
+            a.record(stream)
+            step()
+            b.record(stream)
+            kms.append(z.search_last_ms())
+            nodes += int(d_nd.sum().item())
+        torch.cuda.synchronize()
+    ms = [a.elapsed_time(b) for a, b in ev]
+    scores = d_sc.cpu().numpy().copy()
+    z.search_set_launch_form(0)
+    z.search_set_helpers(0)
+    z.release()
+    total_s = sum(ms) / 1e3
+    nps = nodes / total_s
+    cpu, vals = (None, None) if args.no_cpu else oracle_search_sample(boards, stm, depth)
+    if vals is not None and list(scores[:len(vals)]) != [int(v) for v in vals]:
+        raise SystemExit("batched search root scores differ from the oracle's")
+    return {
+        "metric": f"batched search positions/s (fixed depth {depth}, root score = plain negamax)",
+        "value": round(n * steps / total_s, 2), "unit": "positions/s", "steps": steps, "warmup": 3,
+        "ms_per_step": round(sum(ms) / steps, 3), "kernel_ms": round(sum(kms) / len(kms), 3),
+        "config": {"workload": f"search_batch: {n} playouts of 20-40 plies, >=20 pieces, depth {depth}",
+                   "form": "warp-cooperative", "workers_per_position": SEARCH_WORKERS,
+                   "helper_cap": SEARCH_HELPERS, "tt": "1 GiB, 16-byte entries, cleared every step",
+                   "l2": "the 1 GiB table and 2.4 G node visits per step exceed L2"},
+        "nodes_per_s": round(nps, 1), "nodes_per_step": nodes // steps,
+        "roofline": _node_roofline(z, nps, "ops_per_search_node", "k_search_warp"),
+        "oracle_cpu": cpu, "scores_checked_against_oracle": 0 if vals is None else len(vals),
+        "clocks": clocks.summary(), "gpu_launches": steps * 3,
+    }
+
+
+def learned_ab_block(z, local, rank, args):
+    """Learned vs plain move ordering: iterative deepening 1..8 of the
+    search workload with the hand-written ordering and with the BF16
+    network, interleaved pairs from cleared tables; root scores must be
+    identical, time to depth and nodes are compared."""
+    from zeta_gb300 import learn
+    z.init(local, 1024, 0)
+    boards, stm = _search_arrays(z, rank, args.ab_n or 256)
+    if not learn.load(z):
+        z.release()
+        return {"unavailable": "no trained network (zeta_gb300/models/ordering_params.npy)", "gpu_launches": 0}
+    depth, pairs = args.ab_depth, args.ab_pairs
+    z.search_set_helpers(SEARCH_HELPERS)
+    runs = {0: [], 1: []}
+    identical = True
+    try:
+        with ClockSampler(local) as clocks:
+            for _ in range(pairs):
+                for o in (0, 1):
+                    z.tt_clear()
+                    sc, mv, nodes, ms, ms_s, ms_n = z.search_id(boards, stm, depth, SEARCH_WORKERS, o)
+                    runs[o].append({"ms": ms, "nodes": int(nodes.sum()), "ms_net": ms_n, "scores": sc})
+                identical = identical and np.array_equal(runs[0][-1]["scores"], runs[1][-1]["scores"])
+    finally:
+        z.search_set_helpers(0)
+        z.release()
+
+    def med(o, k):
+        return statistics.median(r[k] for r in runs[o])
+
+    ratio_t = [b["ms"] / a["ms"] for a, b in zip(runs[0], runs[1])]
+    ratio_n = [b["nodes"] / a["nodes"] for a, b in zip(runs[0], runs[1])]
+    return {
+        "metric": f"time to depth {depth}, learned (BF16 network) vs plain ordering, same root scores",
+        "config": {"workload": f"search_batch: {len(stm)} playouts, iterative deepening 1..{depth}",
+                   "form": "automatic (warp-cooperative)", "workers_per_position": SEARCH_WORKERS,
+                   "helper_cap": SEARCH_HELPERS, "pairs": pairs, "order": "plain then learned, interleaved"},
+        "plain": {"ms_median": round(med(0, "ms"), 1), "ms_runs": [round(r["ms"], 1) for r in runs[0]],
+                  "nodes_median": med(0, "nodes"), "nodes_runs": [r["nodes"] for r in runs[0]]},
+        "learned_bf16": {"ms_median": round(med(1, "ms"), 1), "ms_runs": [round(r["ms"], 1) for r in runs[1]],
+                         "nodes_median": med(1, "nodes"), "nodes_runs": [r["nodes"] for r in runs[1]],
+                         "network_ms_median": round(med(1, "ms_net"), 2)},
+        "time_ratio_median": round(statistics.median(ratio_t), 4),
+        "time_ratio_range": [round(min(ratio_t), 4), round(max(ratio_t), 4)],
+        "nodes_ratio_median": round(statistics.median(ratio_n), 4),
+        "nodes_ratio_range": [round(min(ratio_n), 4), round(max(ratio_n), 4)],
+        "scores_identical": bool(identical), "clocks": clocks.summary(),
+        "gpu_launches": pairs * 2 * depth + pairs * (depth - 1) * 4,
+    }
+
+
+def run_learned_ab(args):
+    """The learned-ordering A/B alone, by default on the whole 1024-position
+    search workload at depth 8 (the configured size)."""
+    import torch
+    import zeta_gb300 as z
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    args.ab_n = args.ab_n or 1024
+    block = learned_ab_block(z, local, rank, args)
+    if rank == 0:
+        print(json.dumps(dict(block, n_gpus=world, dtype="int32 search, bf16 network",
+                              data="synthetic (seeded random playouts)")), flush=True)
 
 
 def _ref_lib():
@@ -664,7 +834,14 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--n", type=int, default=0, help="positions per GPU (default: the workload's 4096)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the timed CPU baseline (profiling runs)")
-    ap.add_argument("--workload", choices=["perft_batch", "search_batch", "gemm", "engine", "smp"],
+    ap.add_argument("--no-search", action="store_true",
+                    help="default workload: leave out the batched-search and learned-ordering blocks")
+    ap.add_argument("--ab-n", type=int, default=0,
+                    help="learned-ordering A/B: positions (default: 256 in the default line, 1024 with "
+                         "--workload learned_ab)")
+    ap.add_argument("--ab-depth", type=int, default=8, help="learned-ordering A/B: iterative-deepening depth")
+    ap.add_argument("--ab-pairs", type=int, default=3, help="learned-ordering A/B: interleaved plain/learned pairs")
+    ap.add_argument("--workload", choices=["perft_batch", "search_batch", "learned_ab", "gemm", "engine", "smp"],
                     default="perft_batch")
     ap.add_argument("--depth", type=int, default=0, help="search depth (search_batch; default 7)")
     ap.add_argument("--workers", type=int, default=0, help="ABDADA workers per position (0 = sweep)")
@@ -678,6 +855,8 @@ def main():
         args.warmup = 3
     if args.workload == "search_batch" and args.impl == "ours":
         run_search(args)
+    elif args.workload == "learned_ab" and args.impl == "ours":
+        run_learned_ab(args)
     elif args.workload == "gemm" and args.impl == "ours":
         run_gemm(args)
     elif args.workload == "engine" and args.impl == "ours":

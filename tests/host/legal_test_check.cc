@@ -8,6 +8,9 @@
  *     the same in-check flag;
  *   - the search kernels' generator (gen_engine) gives the perft
  *     generator's (gen_legal) move set, all moves and captures only;
+ *   - the warp generator's plan and per-move decode (warpgen.cuh), in
+ *     both their unrolled and rolled forms, give gen_engine's list move for
+ *     move, in the same order, and the same in-check flag;
  *   - the incremental Zobrist update of the search kernels (parent hash ^
  *     side toggle ^ castle / en-passant keys ^ piece_delta) equals hashing
  *     every child from scratch (compute_hash), and compute_hash equals the
@@ -28,6 +31,7 @@
 #include "../../zeta_gb300/csrc/eval.cuh"
 #include "../../zeta_gb300/csrc/movegen_fast.cuh"
 #include "../../zeta_gb300/csrc/tables.cuh"
+#include "../../zeta_gb300/csrc/warpgen.cuh"
 
 using namespace zeta;
 
@@ -37,6 +41,13 @@ static void walk(const Pos &p, int stm, int depth) {
   bool c1, c2, c3;
   const int n = count_legal_ex(p, stm, c1);
   const bool quick = has_free_move(p, stm, c2);
+  {
+    bool cr;
+    if (has_free_move_rolled(p, stm, cr) != quick || cr != c2) {
+      if (g_bad < 5) printf("rolled quick test differs\n");
+      g_bad++;
+    }
+  }
   const bool has = has_legal_ex(p, stm, c3);
   g_nodes++;
   g_quick += quick;
@@ -55,6 +66,30 @@ static void walk(const Pos &p, int stm, int depth) {
     Move a[256], b[256];
     const int na = gen_legal(p, stm, qs != 0, a);
     const int nb = gen_engine(p, sets, danger, stm, qs != 0, b);
+    {
+      u64 set[kEmitters];
+      bool chk = false;
+      int sqep = 0;
+      const int nw = gen_plan(p, sets, danger, stm, qs != 0, set, &chk, &sqep);
+      uint8_t off[kEmitters + 1];
+      off[0] = 0;
+      for (int e = 0; e < kEmitters; e++) off[e + 1] = (uint8_t)(off[e] + popc(set[e]));
+      bool same = nw == nb && chk == c1 && off[kEmitters] == nw;
+      for (int j = 0; same && j < nw; j++) same = gen_move_at(p, sets, stm, set, off, sqep, j) == b[j];
+      /* the rolled form: the same attack map, sets, flags and list */
+      u64 setr[kEmitters];
+      bool chkr = false;
+      int sqepr = -1;
+      same = same && enemy_attacks_rolled(sets, stm) == danger;
+      const int nr = gen_plan_rolled(p, sets, danger, stm, qs != 0, setr, &chkr, &sqepr);
+      same = same && nr == nw && chkr == chk && sqepr == sqep;
+      for (int e = 0; same && e < kEmitters; e++) same = setr[e] == set[e];
+      for (int j = 0; same && j < nw; j++) same = gen_move_at_rolled(p, sets, stm, setr, off, sqep, j) == b[j];
+      if (!same) {
+        if (g_bad < 5) printf("warp generator differs (qs %d): %d vs %d moves\n", qs, nw, nb);
+        g_bad++;
+      }
+    }
     std::sort(a, a + na);
     std::sort(b, b + nb);
     if (na != nb || !std::equal(a, a + na, b)) {

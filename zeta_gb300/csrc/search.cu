@@ -43,6 +43,7 @@
 #include "eval.cuh"
 #include "movegen_fast.cuh"
 #include "tables.cuh"
+#include "warpgen.cuh"
 
 namespace zeta {
 
@@ -488,7 +489,8 @@ __global__ void __launch_bounds__(TPB) k_search_pure(const uint64_t *__restrict_
 }
 
 /* Hand-off from a warp's tree walker (lane 0) to all 32 lanes: a node with
- * one ply left and its legal moves, in shared memory. */
+ * one ply left, and after its moves are generated, its legal moves (in
+ * shared memory). */
 struct LeafBatch {
   Pos pos;
   int n, ply, beta;
@@ -496,32 +498,297 @@ struct LeafBatch {
   Move moves[kMaxMoves];
 };
 
-/* Captures and promotions to the front of a batch with more than one
- * round of moves, so that the first round holds the moves most likely to
- * reach beta (order among the others kept). */
-__device__ __forceinline__ void batch_captures_first(LeafBatch &B) {
-  if (B.n <= 32) return;
-  int k = 0;
-  for (int i = 0; i < B.n; i++) {
-    const Move mv = B.moves[i];
-    if ((m_pcpt(mv) >> 1) || m_pto(mv) != m_pfrom(mv)) {
-      B.moves[i] = B.moves[k];
-      B.moves[k++] = mv;
+/* Hand-off for generating and ordering the moves of an interior node:
+ * lane 0 puts the position and what orders its moves here; the warp
+ * builds the list (warpgen.cuh), scores it and writes it, best first, to
+ * the node's move array. */
+struct WarpGen {
+  Pos pos;
+  uint32_t stm;
+  Move ttm, k0, k1;
+  int have_l;
+  uint16_t lmv[kOrderTop];
+  int n, chk;
+  u64 set[kEmitters];
+  uint8_t off[kEmitters + 1];
+  int sc[kMaxMoves];
+  Move mv[kMaxMoves];
+  Move srt[kMaxMoves]; /* the ordered list, best first */
+};
+
+constexpr unsigned kFull = 0xFFFFFFFFu;
+
+/* The warp kernel's generator in its rolled form (warpgen.cuh), one
+ * out-of-line copy each: the piece sets, the enemy attack map and the 23
+ * emitter sets of (pos, stm) -- returns the number of legal moves -- and
+ * move j of the list. */
+__device__ __noinline__ int w_plan(const Pos &pos, int stm, u64 *set, bool *chk, int *sqep, Sets *sets) {
+  const Sets s = make_sets(pos, stm);
+  *sets = s;
+  return gen_plan_rolled(pos, s, enemy_attacks_rolled(s, stm), stm, false, set, chk, sqep);
+}
+__device__ __noinline__ Move w_move_at(const Pos &p, const Sets &s, int stm, const u64 *set, const uint8_t *off,
+                                       int sqep, int j) {
+  return gen_move_at_rolled(p, s, stm, set, off, sqep, j);
+}
+
+/* whether the side to move has a legal move, and whether it is in check:
+ * the quick free-move test, then the legal-move count of w_plan (the
+ * generator's own code, so the leaf test adds no second copy of it) */
+__device__ __noinline__ bool w_has_move(const Pos &p, int stm, bool *chk) {
+  bool c;
+  if (has_free_move_rolled(p, stm, c)) {
+    *chk = c;
+    return true;
+  }
+  u64 set[kEmitters];
+  int sqep;
+  Sets s;
+  const int n = w_plan(p, stm, set, chk, &sqep, &s);
+  return n > 0;
+}
+
+/* value of a node with no depth left, from the side to move */
+__device__ __forceinline__ int leaf_value_w(const Pos &p, int stm, int ply, const EvalTables *T) {
+  bool chk;
+  if (!w_has_move(p, stm, &chk)) return chk ? -kSearchInf + ply : 0;
+  const int e = s_eval(p, T);
+  return stm ? -e : e;
+}
+
+/* one ply of a warp worker's stack (lane 0's local memory: its move
+ * flags are written at every visited child, and local memory is cached
+ * write-back) */
+struct WFrame {
+  Pos pos;
+  u64 th;
+  u64 key;
+  int alpha, beta, alpha0, best;
+  Move bestmove;
+  int n, i, iter, searched;
+  int depth;
+  uint8_t stm, exclusive, deferred, busy;
+  Move moves[kMaxMoves];
+};
+
+/* All lanes: the 23 emitter sets of (pos, stm) and their prefix counts into
+ * G; returns the number of legal moves (at most kMaxMoves).  Every lane
+ * computes the same sets (no lane-dependent branch) and writes the same
+ * values to G.set.  One out-of-line copy: the kernel calls it from two
+ * places, and the instruction cache is the search kernels' tightest
+ * resource. */
+__device__ __noinline__ int warp_plan(WarpGen &G, const Pos &pos, int stm, Sets &s, int &sqep, int lane) {
+  bool chk = false;
+  int n = w_plan(pos, stm, G.set, &chk, &sqep, &s);
+  __syncwarp();
+  int c = lane < kEmitters ? popc(G.set[lane]) : 0;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(kFull, c, o);
+    if (lane >= o) c += y;
+  }
+  if (lane < kEmitters) G.off[lane + 1] = (uint8_t)min(c, 255);
+  if (lane == 0) {
+    G.off[0] = 0;
+    G.chk = chk;
+  }
+  __syncwarp();
+  return n < kMaxMoves ? n : kMaxMoves; /* a legal position has at most 218 */
+}
+
+/* All lanes: the moves of G.pos scored as node_enter orders them (table
+ * move, captures by MVV-LVA, promotions, killers, learned ranks, then
+ * piece-square gain) and written to G.srt best first -- a stable sort,
+ * the same order as node_enter's insertion sort: move j goes to the number
+ * of moves with a higher score, or an equal score and a smaller index. */
+__device__ __forceinline__ int warp_gen_order(WarpGen &G, const EvalTables &T, int learned_top, int learned_quiet,
+                                              int lane) {
+  Sets s;
+  int sqep = 0;
+  const Pos pos = G.pos;
+  const int stm = G.stm;
+  const int n = warp_plan(G, pos, stm, s, sqep, lane);
+  const Move ttm = G.ttm, k0 = G.k0, k1 = G.k1;
+  const int have_l = G.have_l;
+  for (int j = lane; j < n; j += 32) {
+    const Move m = w_move_at(pos, s, stm, G.set, G.off, sqep, j);
+    int sc = order_score(m, stm, ttm, k0, k1, T);
+    if (have_l && m != ttm) {
+      const int r = learned_rank(G.lmv, m);
+      if (r >= 0 && r < learned_top) {
+        if (!learned_quiet)
+          sc = (1 << 19) - r;
+        else if (sc < (1 << 16))
+          sc = (1 << 15) - r; /* below captures, promotions and killers */
+      }
+    }
+    G.sc[j] = sc;
+    G.mv[j] = m;
+  }
+  __syncwarp();
+  for (int j = lane; j < n; j += 32) {
+    const int sj = G.sc[j];
+    int r = 0;
+    for (int i = 0; i < n; i++) {
+      const int si = G.sc[i];
+      r += (si > sj) || (si == sj && i < j);
+    }
+    G.srt[r] = G.mv[j];
+  }
+  if (lane == 0) G.n = n;
+  __syncwarp(); /* the list and G.n are visible to lane 0 */
+  return n;
+}
+
+/* All lanes: the legal moves of B.pos into B.moves, captures and
+ * promotions first when they take more than one scoring round (each group
+ * in generation order). */
+__device__ __forceinline__ int warp_gen_batch(WarpGen &G, LeafBatch &B, int lane) {
+  Sets s;
+  int sqep = 0;
+  const Pos pos = B.pos;
+  const int stm = B.stm;
+  const int n = warp_plan(G, pos, stm, s, sqep, lane);
+  if (n <= 32) {
+    if (lane < n) B.moves[lane] = w_move_at(pos, s, stm, G.set, G.off, sqep, lane);
+  } else {
+    int ncap = 0;
+    for (int base = 0; base < n; base += 32) {
+      const int j = base + lane;
+      bool cap = false;
+      if (j < n) {
+        const Move m = w_move_at(pos, s, stm, G.set, G.off, sqep, j);
+        cap = (m_pcpt(m) >> 1) || m_pto(m) != m_pfrom(m);
+        G.mv[j] = m;
+      }
+      ncap += __popc(__ballot_sync(kFull, cap));
+    }
+    __syncwarp();
+    const unsigned lt = (1u << lane) - 1u;
+    int ci = 0, qi = ncap;
+    for (int base = 0; base < n; base += 32) {
+      const int j = base + lane;
+      const Move m = j < n ? G.mv[j] : 0u;
+      const bool cap = j < n && ((m_pcpt(m) >> 1) || m_pto(m) != m_pfrom(m));
+      const unsigned bc = __ballot_sync(kFull, cap), bq = __ballot_sync(kFull, j < n && !cap);
+      if (j < n) B.moves[cap ? ci + __popc(bc & lt) : qi + __popc(bq & lt)] = m;
+      ci += __popc(bc);
+      qi += __popc(bq);
     }
   }
+  if (lane == 0) B.n = n;
+  __syncwarp();
+  return n;
+}
+
+/* lane 0: node entry up to move generation -- table probe (a move from any
+ * depth orders, only an equal depth cuts), the ABDADA busy check, the
+ * learned-ordering lookup or request.  false: decided here (`value`;
+ * kOnEval for a busy node asked exclusively).  true: the moves must be
+ * generated; the request is in G. */
+__device__ bool wnode_pre(Worker &W, WFrame &f, int ply, int &value, WarpGen &G) {
+  W.nodes++;
+  f.key = search_key(f.pos, f.th);
+  Move ttm = 0;
+  int ts, td, tb;
+  Move tm;
+  if (tt_probe(W.tt, W.tt_mask, f.key, ts, td, tb, tm)) {
+    ttm = tm;
+    if (td == f.depth) {
+      const int s = from_tt(ts, ply);
+      if (ply > 0 && (tb == B_EXACT || (tb == B_LOWER && s >= f.beta) || (tb == B_UPPER && s <= f.alpha))) {
+        W.tthits++;
+        value = s;
+        return false;
+      }
+    }
+  }
+  const u64 bidx = (f.key >> 32) & W.busy_mask;
+  if (f.exclusive && f.depth >= kAbdadaMinDepth && ((volatile uint32_t *)W.busy)[bidx] > 0) {
+    value = kOnEval;
+    return false;
+  }
+  G.have_l = 0;
+  if (W.learned && f.depth >= 2) {
+    OrderEntry *e = &W.ocache[f.key & W.ocache_mask];
+    const unsigned long long ek = ((volatile unsigned long long *)&e->key)[0];
+    if (ek == f.key) {
+      if (f.depth >= 3) {
+#pragma unroll
+        for (int r = 0; r < kOrderTop; r++) G.lmv[r] = e->mv[r];
+        G.have_l = 1;
+      }
+    } else {
+      const uint32_t idx = atomicAdd(W.noreq, 1u);
+      if (idx < W.oreq_cap) {
+        OrderRequest q;
+        q.key = f.key;
+        q.b[0] = f.pos.b0;
+        q.b[1] = f.pos.p1;
+        q.b[2] = f.pos.p2;
+        q.b[3] = f.pos.p3;
+        q.b[4] = f.pos.cr;
+        q.stm = f.stm;
+        q.pad = 0;
+        W.oreq[idx] = q;
+        OrderEntry pend;
+        pend.key = f.key;
+#pragma unroll
+        for (int r = 0; r < kOrderTop; r++) pend.mv[r] = 0xFFFF;
+        *e = pend;
+      }
+    }
+  }
+  G.pos = f.pos;
+  G.stm = f.stm;
+  G.ttm = ttm;
+  G.k0 = W.killer[ply][0];
+  G.k1 = W.killer[ply][1];
+  return true;
+}
+
+/* lane 0: node entry after the warp generated and ordered n moves.  false:
+ * no legal move (`value` = mate or stalemate score). */
+__device__ bool wnode_post(Worker &W, WFrame &f, int ply, const Move *srt, int n, bool chk, int &value) {
+  f.n = n;
+  for (int i = 0; i < n; i++) f.moves[i] = srt[i];
+  if (n == 0) {
+    value = chk ? -kSearchInf + ply : 0;
+    return false;
+  }
+  f.busy = f.depth >= kAbdadaMinDepth;
+  if (f.busy) atomicAdd(&W.busy[(f.key >> 32) & W.busy_mask], 1u);
+  f.best = -kSearchInf - 1;
+  f.bestmove = 0;
+  f.alpha0 = f.alpha;
+  f.i = f.iter = f.searched = 0;
+  f.deferred = 0;
+  return true;
+}
+
+__device__ __forceinline__ int wnode_finish(Worker &W, WFrame &f, int ply) {
+  if (f.busy) atomicSub(&W.busy[(f.key >> 32) & W.busy_mask], 1u);
+  const int bound = f.best <= f.alpha0 ? B_UPPER : (f.best >= f.beta ? B_LOWER : B_EXACT);
+  tt_store(W.tt, W.tt_mask, f.key, to_tt(f.best, ply), f.depth, bound, f.bestmove);
+  return f.best;
 }
 
 /* Warp-cooperative form: one warp is one ABDADA worker.  Lane 0 walks the
- * tree as k_search_pure does down to the nodes with one ply left; the
- * children of such a node are then played and scored by all 32 lanes at
- * once, 32 moves per round (lane i takes move r * 32 + i in round r), and
- * a warp reduction after each round gives the best value so far.  A round
- * whose best reaches the node's beta ends the node with that lower bound;
- * a node whose moves were all scored has its exact value.  Either is
- * stored in the table as such, so only the number of leaves visited
- * changes and the root value is plain negamax as before.  The nodes with
- * two or more plies left (move ordering, ABDADA, the table, killers, the
- * learned ordering) are the k_search_pure walk unchanged. */
+ * tree with the control flow of k_search_pure (same ordering, table,
+ * ABDADA, killers, learned ordering); all 32 lanes do the per-node work:
+ *  - at a node with two or more plies left, the warp generates the legal
+ *    moves (warpgen.cuh), scores them and sorts them into the node's move
+ *    array -- the same list, in the same order, as k_search_pure's;
+ *  - at a node with one ply left, the warp generates its moves and then
+ *    plays and scores the children, 32 per round (lane i takes move r*32+i
+ *    in round r), with a warp reduction after each round.  A round whose
+ *    best value reaches the node's beta ends the node with that lower
+ *    bound; a node whose moves were all scored has its exact value.
+ *    Either is stored in the table as such, so only the number of leaves
+ *    visited changes and the root value is plain negamax.
+ * Lane 0 hands work to the warp with a command: 2 generate and order the
+ * moves of the node in G (lane 0 then copies the list into its frame), 3
+ * generate and score the batch in B, 0 stop. */
 template <int TPB>
 __global__ void __launch_bounds__(TPB, 4) k_search_warp(const uint64_t *__restrict__ boards, const uint8_t *__restrict__ stm,
                                                      int N, int nworkers, int depth, TTEntry *tt, u64 tt_mask,
@@ -530,6 +797,7 @@ __global__ void __launch_bounds__(TPB, 4) k_search_warp(const uint64_t *__restri
                                                      int max_per_pos, LearnArgs la) {
   __shared__ EvalTables sT;
   __shared__ LeafBatch LB[TPB / 32];
+  __shared__ WarpGen WG[TPB / 32];
   for (int i = threadIdx.x; i < (int)(sizeof(EvalTables) / 4); i += TPB)
     ((uint32_t *)&sT)[i] = ((const uint32_t *)&kEvalDev)[i];
   __syncthreads();
@@ -537,8 +805,9 @@ __global__ void __launch_bounds__(TPB, 4) k_search_warp(const uint64_t *__restri
   const long long t = ((long long)blockIdx.x * TPB + threadIdx.x) >> 5; /* worker = warp */
   if (t >= (long long)N * nworkers) return;                              /* whole warps leave */
   LeafBatch &B = LB[threadIdx.x >> 5];
+  WarpGen &G = WG[threadIdx.x >> 5];
 
-  Frame F[kMaxSearchDepth + 1]; /* lane 0's stack; the other lanes never touch theirs */
+  WFrame F[kMaxSearchDepth + 1]; /* lane 0's stack; the other lanes never touch theirs */
   Worker W;
   W.tt = tt;
   W.tt_mask = tt_mask;
@@ -555,12 +824,13 @@ __global__ void __launch_bounds__(TPB, 4) k_search_warp(const uint64_t *__restri
   W.oreq_cap = la.cap;
   unsigned long long steps = 0;
   int p = (int)(t % N), job = 0, ply = 0;
-  int phase = 0; /* lane 0: 0 take a job, 1 walk, 2 take a batch's value */
+  int phase = 0; /* lane 0: 0 take a job, 1 walk, 2 take a batch's value, 3 finish a node entry */
   int pend = 0;  /* the batch is 1: the child F[ply + 1], 2: the root */
+  int gq = 0;    /* phase 3: the frame whose moves the warp generated */
   int bval = 0, bidx = 0, bdone = 0;
 
   for (;;) {
-    int cmd = 0; /* 0: the worker stops; 1: score the batch in B */
+    int cmd = 0; /* 0: the worker stops; 2: generate and order frame gq; 3: generate and score B */
     if (lane == 0) {
       for (;;) {
         if (++steps > budget) {
@@ -605,62 +875,89 @@ __global__ void __launch_bounds__(TPB, 4) k_search_warp(const uint64_t *__restri
           F[0].alpha = -kSearchInf - 1;
           F[0].beta = kSearchInf + 1;
           F[0].exclusive = 0;
-          int v = 0;
-          bool open = false;
           if (depth == 1) {
             W.nodes++;
             F[0].key = search_key(F[0].pos, F[0].th);
-            B.n = s_gen(F[0].pos, F[0].stm, B.moves);
-            if (B.n > 0) {
-              B.pos = F[0].pos;
-              B.stm = F[0].stm;
-              B.ply = 0;
-              B.beta = kSearchInf + 1;
-              pend = 2;
-              phase = 2;
-              cmd = 1;
-              break;
-            }
-            bool chk;
-            s_count(F[0].pos, F[0].stm, &chk);
-            v = chk ? -kSearchInf : 0;
-          } else {
-            open = node_enter(W, F[0], 0, v);
+            B.pos = F[0].pos;
+            B.stm = F[0].stm;
+            B.ply = 0;
+            B.beta = kSearchInf + 1;
+            pend = 2;
+            phase = 2;
+            cmd = 3;
+            break;
           }
-          if (!open) {
-            /* no legal move at the root: the game is over */
-            if (atomicCAS(&done[p], 0u, 1u) == 0u) {
-              out[p].score = v;
-              out[p].bestmove = 0;
-            }
-            atomicAdd(&out[p].nodes, W.nodes);
-            atomicSub(&active[p], 1u);
-            continue;
+          int v = 0;
+          if (wnode_pre(W, F[0], 0, v, G)) {
+            gq = 0;
+            phase = 3;
+            cmd = 2;
+            break;
           }
-          ply = 0;
-          phase = 1;
+          /* the root is never cut or deferred on entry */
+          atomicAdd(&out[p].nodes, W.nodes);
+          atomicSub(&active[p], 1u);
           continue;
         }
-        if (phase == 2) {
-          /* the lanes scored every child of the batch node */
+        if (phase == 3) {
+          /* the warp generated and ordered frame gq's moves */
           phase = 1;
-          W.nodes += bdone;
-          const Move bm = B.moves[bidx];
-          if (pend == 2) {
-            tt_store(W.tt, W.tt_mask, F[0].key, bval, 1, B_EXACT, bm);
-            if (atomicCAS(&done[p], 0u, 1u) == 0u) {
-              out[p].score = bval;
-              out[p].bestmove = bm;
+          int v = 0;
+          const bool open = wnode_post(W, F[gq], gq, G.srt, G.n, G.chk != 0, v);
+          if (gq == 0) {
+            if (!open) {
+              /* no legal move at the root: the game is over */
+              if (atomicCAS(&done[p], 0u, 1u) == 0u) {
+                out[p].score = v;
+                out[p].bestmove = 0;
+              }
+              atomicAdd(&out[p].nodes, W.nodes);
+              atomicSub(&active[p], 1u);
+              phase = 0;
             }
-            atomicAdd(&out[p].nodes, W.nodes);
-            atomicAdd(&out[p].tthits, W.tthits);
-            atomicSub(&active[p], 1u);
-            phase = 0;
+            ply = 0;
             continue;
           }
-          tt_store(W.tt, W.tt_mask, F[ply + 1].key, to_tt(bval, ply + 1), 1, bdone == B.n ? B_EXACT : B_LOWER,
-                   bm);
-          val = -bval;
+          if (open) {
+            ply = gq;
+            continue;
+          }
+          val = -v; /* a child with no legal move: falls through to its parent F[ply] */
+        } else if (phase == 2) {
+          /* the lanes scored every child of the batch node (or it has none) */
+          phase = 1;
+          W.nodes += bdone;
+          if (B.n == 0) {
+            const int mate = G.chk ? -kSearchInf + B.ply : 0;
+            if (pend == 2) {
+              if (atomicCAS(&done[p], 0u, 1u) == 0u) {
+                out[p].score = mate;
+                out[p].bestmove = 0;
+              }
+              atomicAdd(&out[p].nodes, W.nodes);
+              atomicSub(&active[p], 1u);
+              phase = 0;
+              continue;
+            }
+            val = -mate;
+          } else {
+            const Move bm = B.moves[bidx];
+            if (pend == 2) {
+              tt_store(W.tt, W.tt_mask, F[0].key, bval, 1, B_EXACT, bm);
+              if (atomicCAS(&done[p], 0u, 1u) == 0u) {
+                out[p].score = bval;
+                out[p].bestmove = bm;
+              }
+              atomicAdd(&out[p].nodes, W.nodes);
+              atomicAdd(&out[p].tthits, W.tthits);
+              atomicSub(&active[p], 1u);
+              phase = 0;
+              continue;
+            }
+            tt_store(W.tt, W.tt_mask, F[ply + 1].key, to_tt(bval, ply + 1), 1, bdone == B.n ? B_EXACT : B_LOWER,
+                     bm);
+            val = -bval;
+          }
         } else {
           if ((steps & 15) == 0 && ((volatile uint32_t *)done)[p]) {
             /* another worker finished this position */
@@ -670,7 +967,7 @@ __global__ void __launch_bounds__(TPB, 4) k_search_warp(const uint64_t *__restri
             phase = 0;
             continue;
           }
-          Frame &f = F[ply];
+          WFrame &f = F[ply];
           while (f.i < f.n && ((f.moves[f.i] & kDone) || (f.iter == 1 && !(f.moves[f.i] & kDefer)))) f.i++;
           if (f.i >= f.n) {
             if (f.iter == 0 && f.deferred) {
@@ -679,7 +976,7 @@ __global__ void __launch_bounds__(TPB, 4) k_search_warp(const uint64_t *__restri
               f.deferred = 0;
               continue;
             }
-            const int r = node_finish(W, f, ply);
+            const int r = wnode_finish(W, f, ply);
             if (ply == 0) {
               if (atomicCAS(&done[p], 0u, 1u) == 0u) {
                 out[p].score = r;
@@ -695,7 +992,7 @@ __global__ void __launch_bounds__(TPB, 4) k_search_warp(const uint64_t *__restri
             val = -r;
           } else {
             const Move m = f.moves[f.i] & kMoveBits;
-            Frame &g = F[ply + 1];
+            WFrame &g = F[ply + 1];
             g.pos = f.pos;
             play(g.pos, m, false);
             g.th = f.th ^ 1ULL ^ cr_keys(f.pos.cr) ^ cr_keys(g.pos.cr) ^ piece_delta(m);
@@ -705,7 +1002,7 @@ __global__ void __launch_bounds__(TPB, 4) k_search_warp(const uint64_t *__restri
             g.beta = -(f.alpha > f.best ? f.alpha : f.best);
             g.exclusive = (f.iter == 0 && f.searched > 0);
             if (g.depth == 1) {
-              /* one ply left: a table hit, no legal move, or a batch */
+              /* one ply left: a table hit, or a batch for the warp */
               W.nodes++;
               g.key = search_key(g.pos, g.th);
               int ts, td, tb;
@@ -720,27 +1017,22 @@ __global__ void __launch_bounds__(TPB, 4) k_search_warp(const uint64_t *__restri
                 }
               }
               if (!hit) {
-                B.n = s_gen(g.pos, g.stm, B.moves);
-                if (B.n > 0) {
-                  batch_captures_first(B);
-                  B.pos = g.pos;
-                  B.stm = g.stm;
-                  B.ply = ply + 1;
-                  B.beta = g.beta;
-                  pend = 1;
-                  phase = 2;
-                  cmd = 1;
-                  break;
-                }
-                bool chk;
-                s_count(g.pos, g.stm, &chk);
-                val = chk ? kSearchInf - (ply + 1) : 0;
+                B.pos = g.pos;
+                B.stm = g.stm;
+                B.ply = ply + 1;
+                B.beta = g.beta;
+                pend = 1;
+                phase = 2;
+                cmd = 3;
+                break;
               }
             } else {
-              int cv;
-              if (node_enter(W, g, ply + 1, cv)) {
-                ply++;
-                continue;
+              int cv = 0;
+              if (wnode_pre(W, g, ply + 1, cv, G)) {
+                gq = ply + 1;
+                phase = 3;
+                cmd = 2;
+                break;
               }
               if (cv == kOnEval) deferred = true;
               else val = -cv;
@@ -748,7 +1040,7 @@ __global__ void __launch_bounds__(TPB, 4) k_search_warp(const uint64_t *__restri
           }
         }
         /* a child of F[ply] returned `val` (or was deferred) */
-        Frame &h = F[ply];
+        WFrame &h = F[ply];
         if (deferred) {
           h.moves[h.i] |= kDefer;
           h.deferred = 1;
@@ -774,28 +1066,34 @@ __global__ void __launch_bounds__(TPB, 4) k_search_warp(const uint64_t *__restri
         }
       }
     }
-    cmd = __shfl_sync(0xffffffffu, cmd, 0);
+    cmd = __shfl_sync(kFull, cmd, 0);
     if (!cmd) break;
-    __syncwarp(); /* lane 0's batch is visible to the warp */
-    const int n = B.n, beta = B.beta;
+    __syncwarp(); /* lane 0's request in G or B is visible to the warp */
+    if (cmd == 2) {
+      warp_gen_order(G, sT, W.learned_top, W.learned_quiet, lane);
+      continue;
+    }
+    /* cmd 3: generate the batch node's moves, then score its children */
+    const int n = warp_gen_batch(G, B, lane);
+    const int beta = B.beta;
     int best = -kSearchInf - 1, bi = 0, scored = 0;
     for (int base = 0; base < n; base += 32) {
       const int i = base + lane;
       if (i < n) {
         Pos c = B.pos;
         play(c, B.moves[i], false);
-        const int v = -leaf_value(c, B.stm ^ 1, B.ply + 1, &sT);
+        const int v = -leaf_value_w(c, B.stm ^ 1, B.ply + 1, &sT);
         if (v > best) {
           best = v;
           bi = i;
         }
       }
-      /* the best value so far, the first move in generation order on ties;
+      /* the best value so far, the first move in list order on ties;
        * every lane ends with the same pair */
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {
-        const int ov = __shfl_xor_sync(0xffffffffu, best, o);
-        const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+        const int ov = __shfl_xor_sync(kFull, best, o);
+        const int oi = __shfl_xor_sync(kFull, bi, o);
         if (ov > best || (ov == best && oi < bi)) {
           best = ov;
           bi = oi;
