@@ -41,6 +41,24 @@ def test_engine_startpos_matches_reference(zeta_device):
     assert np.int32(pv[0]) == 0 and cnt[0, 1] == 16392
 
 
+def test_engine_depth0_warmup_matches_reference(zeta_device):
+    """The reference host's start-up launch cl_run_alphabeta(stm, 0, 1)
+    (src/zeta.c:695): a quiescence search of the root, with and without the
+    one-node budget, equal to the reference kernel's PV and counters."""
+    _need_reference()
+    w = zeta_device.WORKLOADS["engine"]
+    boards, stm, _ = ol.make_positions(w["seed"], 5, min_plies=w["min_plies"], max_plies=w["max_plies"],
+                                       min_pieces=w["min_pieces"], min_depth=0, max_depth=0)
+    start, s0 = ol.setboard("rnbqkbnr/pppppppp/8/8/8/8/PPPPPPPP/RNBQKBNR w KQkq - 0 1")
+    for b, s in [(start, s0)] + list(zip(boards, stm)):
+        for max_nodes in (1, 1 << 40):
+            ref = ol.RefSearch(E1, E2)
+            zeta_device.tt_clear()
+            pv_r, c_r = ref.run(b, int(s), 0, max_nodes=max_nodes)
+            pv_g, c_g = zeta_device.engine_search(b, int(s), 0, 1, max_nodes=max_nodes)
+            assert list(pv_g) == list(pv_r) and list(c_g[0, SLOTS]) == list(c_r[0, SLOTS]), max_nodes
+
+
 @pytest.mark.parametrize("i", range(6))
 def test_engine_middlegames_match_reference(zeta_device, i):
     _need_reference()
