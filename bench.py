@@ -271,8 +271,7 @@ def run_ours(args):
         "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(sum(step_ms) / len(step_ms), 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic (seeded random playouts)",
-        "config": {"workload": f"{WORKLOAD}: {n} seeded playouts of 10-60 plies, perft depth U[3,5]",
-                   "positions_per_gpu": n, "leaves_per_step_per_gpu": int(ref_counts.sum()),
+        "config": {**perft_config(n), "leaves_per_step_per_gpu": int(ref_counts.sum()),
                    "l2": "flushed between timed steps (256 MB write)", "parallelism": f"replicas x{world}",
                    "perft_config": z.perft_config()},
         "e2e": {"value": round(e2e_value, 1), "unit": UNIT, "h2d_bytes_per_step": n * 58,
@@ -293,11 +292,14 @@ def run_ours(args):
     z.release()
 
 
-# The batched-search setting of the default line: the warp-cooperative form
-# with 2 ABDADA workers per position and finished workers helping the
-# unfinished positions up to 64 workers each (the fastest setting of the
-# --workload search_batch sweep).
-SEARCH_FORM, SEARCH_WORKERS, SEARCH_HELPERS = 3, 2, 64
+def _search_setting():
+    """(launch form, ABDADA workers per position, helper cap) of the default
+    line's batched search: the autotuner's record (python -m
+    zeta_gb300.autotune search), else warp-cooperative, 2 workers, helpers
+    up to 64 per position.  The table stays at the configured 1 GiB."""
+    from zeta_gb300.autotune import load_search_tuned
+    t = load_search_tuned()
+    return t["form"], t["workers"], t["helpers"]
 
 
 def _search_arrays(z, rank, n):
@@ -347,12 +349,13 @@ def search_batch_block(z, local, rank, args):
     d_mv = torch.zeros(n, dtype=torch.int32, device=dev)
     d_nd = torch.zeros(n, dtype=torch.int64, device=dev)
     stream = torch.cuda.Stream(dev)
-    z.search_set_launch_form(SEARCH_FORM)
-    z.search_set_helpers(SEARCH_HELPERS)
+    s_form, s_workers, s_helpers = _search_setting()
+    z.search_set_launch_form(s_form)
+    z.search_set_helpers(s_helpers)
 
     def step():
         z.tt_clear()
-        z.search_batch_device(d_b.data_ptr(), d_s.data_ptr(), n, depth, SEARCH_WORKERS, d_sc.data_ptr(),
+        z.search_batch_device(d_b.data_ptr(), d_s.data_ptr(), n, depth, s_workers, d_sc.data_ptr(),
                               d_mv.data_ptr(), d_nd.data_ptr(), stream.cuda_stream)
 
     for _ in range(3):
@@ -384,8 +387,9 @@ def search_batch_block(z, local, rank, args):
         "value": round(n * steps / total_s, 2), "unit": "positions/s", "steps": steps, "warmup": 3,
         "ms_per_step": round(sum(ms) / steps, 3), "kernel_ms": round(sum(kms) / len(kms), 3),
         "config": {"workload": f"search_batch: {n} playouts of 20-40 plies, >=20 pieces, depth {depth}",
-                   "form": "warp-cooperative", "workers_per_position": SEARCH_WORKERS,
-                   "helper_cap": SEARCH_HELPERS, "tt": "1 GiB, 16-byte entries, cleared every step",
+                   "form": {1: "dense", 2: "sparse", 3: "warp-cooperative"}.get(s_form, "automatic"),
+                   "workers_per_position": s_workers,
+                   "helper_cap": s_helpers, "tt": "1 GiB, 16-byte entries, cleared every step",
                    "l2": "the 1 GiB table and 2.4 G node visits per step exceed L2"},
         "nodes_per_s": round(nps, 1), "nodes_per_step": nodes // steps,
         "roofline": _node_roofline(z, nps, "ops_per_search_node", "k_search_warp"),
@@ -406,7 +410,8 @@ def learned_ab_block(z, local, rank, args):
         z.release()
         return {"unavailable": "no trained network (zeta_gb300/models/ordering_params.npy)", "gpu_launches": 0}
     depth, pairs = args.ab_depth, args.ab_pairs
-    z.search_set_helpers(SEARCH_HELPERS)
+    _, s_workers, s_helpers = _search_setting()
+    z.search_set_helpers(s_helpers)
     runs = {0: [], 1: []}
     identical = True
     try:
@@ -414,7 +419,7 @@ def learned_ab_block(z, local, rank, args):
             for _ in range(pairs):
                 for o in (0, 1):
                     z.tt_clear()
-                    sc, mv, nodes, ms, ms_s, ms_n = z.search_id(boards, stm, depth, SEARCH_WORKERS, o)
+                    sc, mv, nodes, ms, ms_s, ms_n = z.search_id(boards, stm, depth, s_workers, o)
                     runs[o].append({"ms": ms, "nodes": int(nodes.sum()), "ms_net": ms_n, "scores": sc})
                 identical = identical and np.array_equal(runs[0][-1]["scores"], runs[1][-1]["scores"])
     finally:
@@ -429,8 +434,8 @@ def learned_ab_block(z, local, rank, args):
     return {
         "metric": f"time to depth {depth}, learned (BF16 network) vs plain ordering, same root scores",
         "config": {"workload": f"search_batch: {len(stm)} playouts, iterative deepening 1..{depth}",
-                   "form": "automatic (warp-cooperative)", "workers_per_position": SEARCH_WORKERS,
-                   "helper_cap": SEARCH_HELPERS, "pairs": pairs, "order": "plain then learned, interleaved"},
+                   "form": "automatic (warp-cooperative)", "workers_per_position": s_workers,
+                   "helper_cap": s_helpers, "pairs": pairs, "order": "plain then learned, interleaved"},
         "plain": {"ms_median": round(med(0, "ms"), 1), "ms_runs": [round(r["ms"], 1) for r in runs[0]],
                   "nodes_median": med(0, "nodes"), "nodes_runs": [r["nodes"] for r in runs[0]]},
         "learned_bf16": {"ms_median": round(med(1, "ms"), 1), "ms_runs": [round(r["ms"], 1) for r in runs[1]],
@@ -467,29 +472,37 @@ def _ref_lib():
     return ol, ol.reference()
 
 
-def cpu_baseline_sample(boards, stm, depth, budget_s: float = 12.0):
+def perft_config(n: int) -> dict:
+    """The batched-perft workload, as both arms of the bench name it."""
+    return {"workload": f"{WORKLOAD}: {n} seeded playouts of 10-60 plies, perft depth U[3,5]",
+            "positions_per_gpu": n}
+
+
+def reference_sample_size(cores: int) -> int:
+    """Positions per sample of the reference perft kernel on the host: four
+    per thread, so that every thread stays busy to the end."""
+    return 4 * cores
+
+
+def cpu_baseline_sample(boards, stm, depth):
     """The reference perft kernel on the host cores, on a bounded sample of
-    the workload: the first positions at depth 3 (leaves/s does not depend
-    on depth for a kernel that visits every leaf)."""
+    the workload: the first 4 x threads positions at depth 3 (leaves/s does
+    not depend on depth for a kernel that visits every leaf) -- the same
+    sample as each step of --impl reference."""
     ol, ref = _ref_lib()
     if ref is None:
         return {"value": None, "unit": UNIT, "cores": 0, "kind": "reference",
                 "sample": "reference kernels not built on this host"}
     cores = os.cpu_count() or 1
-    k = cores
-    total_leaves, total_s = 0, 0.0
-    while total_s < budget_s and k <= len(depth):
-        d3 = np.full(k, 3, dtype=np.int32)
-        t0 = time.perf_counter()
-        out = ol.ref_perft_batch(boards[:k], stm[:k], d3, cores)
-        dt = time.perf_counter() - t0
-        total_leaves, total_s = int(out.sum()), dt
-        if dt > budget_s / 3:
-            break
-        k = min(len(depth), k * 2) if k < len(depth) else k + 1
-    return {"value": round(total_leaves / total_s, 1), "unit": UNIT, "cores": cores, "kind": "reference",
+    k = min(len(depth), reference_sample_size(cores))
+    d3 = np.full(k, 3, dtype=np.int32)
+    t0 = time.perf_counter()
+    out = ol.ref_perft_batch(boards[:k], stm[:k], d3, cores)
+    dt = time.perf_counter() - t0
+    leaves = int(out.sum())
+    return {"value": round(leaves / dt, 1), "unit": UNIT, "cores": cores, "kind": "reference",
             "sample": f"unmodified zetaperft.cl on {cores} host threads (64-lane work-group emulator), "
-                      f"first {k} workload positions at depth 3, {total_leaves} leaves in {total_s:.1f}s"}
+                      f"first {k} workload positions at depth 3, {leaves} leaves in {dt:.1f}s"}
 
 
 def run_search(args):
@@ -801,7 +814,7 @@ def run_reference(args):
                                            min_pieces=w["min_pieces"], min_depth=w["min_depth"],
                                            max_depth=w["max_depth"])
     cores = os.cpu_count() or 1
-    k = 2 * cores
+    k = reference_sample_size(cores)
     d3 = np.full(k, 3, dtype=np.int32)
     for _ in range(args.warmup):
         ol.ref_perft_batch(boards[:cores], stm[:cores], d3[:cores], cores)
@@ -819,7 +832,7 @@ def run_reference(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t_total / args.steps * 1e3, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
         "data": "synthetic (seeded random playouts)",
-        "config": {"workload": f"{WORKLOAD}: seeded playouts of 10-60 plies (bounded sample at depth 3)"},
+        "config": perft_config(w["n"]),
         "cpu_baseline": {"value": round(value, 1), "unit": UNIT, "cores": cores, "kind": "reference",
                          "sample": sample},
         "e2e": {"value": round(value, 1), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},

@@ -57,6 +57,13 @@ clrun_bool cl_guess_config(clrun_bool extreme);
 clrun_bool cl_platform_list(void);
 clrun_bool cl_device_list(void);
 
+/* The file cl_guess_config writes: config.txt keys in the reference's
+ * format (src/clconfig.c:784-804), which the reference's
+ * read_and_init_config (src/io.c:533-583) and this project's host read
+ * back.  Returns 1 on success. */
+clrun_bool clrun_write_config(const char *path, uint64_t workers, uint64_t nps, uint64_t tt1_mb, uint64_t tt2_mb,
+                              int32_t device, const char *note);
+
 /* No counterpart in the reference: makes cl_run_alphabeta run the pure
  * fixed-depth search (root score = plain negamax) instead of the
  * reference's search with its heuristics (the default). */

@@ -93,6 +93,42 @@ def test_host_board_layer_survives_malformed_fens(tmp_path):
         assert int(f[0]) == int(one_each), line
 
 
+CONFIG_HARNESS = r"""
+#include <inttypes.h>
+#include <stdio.h>
+#include "engine.h"
+int main(int argc, char **argv) {
+  if (!clrun_write_config(argv[1], 384, 26000000, 2048, 64, 3, "a test device")) return 2;
+  if (!read_config(argv[1])) return 3;
+  printf("%" PRIu64 " %" PRIu64 " %" PRIi64 " %" PRIu64 " %" PRIu64 " %" PRIu64 " %d\n", threadsX, totalWorkUnits,
+         nodes_per_second, MaxNodes, tt1_memory, tt2_memory, opencl_device_id);
+  return 0;
+}
+"""
+
+
+def test_config_file_round_trip(tmp_path):
+    """What the tuner (cl_guess_config) writes, in the reference's config.txt
+    key format, is what the host's read_config applies at start-up:
+    workers, node rate (and the node budget from it), table sizes, device."""
+    lib = os.path.join(ROOT, "zeta_gb300", "_build")
+    if not os.path.exists(os.path.join(lib, "libzeta_cuda.so")):
+        pytest.skip("libzeta_cuda.so not built")
+    src = tmp_path / "cfg.c"
+    src.write_text(CONFIG_HARNESS)
+    exe = tmp_path / "cfg"
+    subprocess.run(["gcc", "-O1", "-std=gnu11", "-I", HOST, "-I", os.path.join(ROOT, "include"), "-o", str(exe),
+                    str(src), os.path.join(HOST, "cudarun.c"), os.path.join(HOST, "engine.c"),
+                    os.path.join(HOST, "board.c"), "-L", lib, "-lzeta_cuda", "-Wl,-rpath," + lib, "-lm"], check=True)
+    cfg = tmp_path / "config.txt"
+    r = subprocess.run([str(exe), str(cfg)], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0, r.stderr
+    assert r.stdout.split() == ["384", "384", "26000000", "26000000", "2048", "64", "3"]
+    text = cfg.read_text()
+    for key in ("threadsX:", "threadsY:", "nodes_per_second:", "tt1_memory:", "tt2_memory:", "opencl_device_id:"):
+        assert key in text
+
+
 def test_zeta_binary_help_runs_without_gpu():
     if not os.path.exists(ZETA):
         pytest.skip("host binary not built")

@@ -189,22 +189,34 @@ clrun_bool cl_guess_config(clrun_bool extreme) {
     }
   }
   zeta_release();
-  FILE *cfg = fopen("config.txt", "w");
-  if (!cfg) {
+  char note[128];
+  snprintf(note, sizeof note, "CUDA device %d (compute capability %d.%d, %d SMs)", opencl_device_id, major, minor,
+           sms);
+  if (!clrun_write_config("config.txt", (uint64_t)best_w, best_nps, t1, 0, opencl_device_id, note)) {
     fprintf(stderr, "Error: cannot write config.txt\n");
     return 0;
   }
+  printf("#> ### config.txt written: %d workers, %.3f s to depth %d ###\n", best_w, best_s, depth);
+  return 1;
+}
+
+/* config.txt in the reference's key format (src/clconfig.c:784-804, read
+ * back by src/io.c:533-583): threadsX x threadsY workers, node rate, table
+ * sizes, device */
+clrun_bool clrun_write_config(const char *path, uint64_t workers, uint64_t nps, uint64_t tt1_mb, uint64_t tt2_mb,
+                              int32_t device, const char *note) {
+  FILE *cfg = fopen(path, "w");
+  if (!cfg) return 0;
   fprintf(cfg, "################################################################################\n");
-  fprintf(cfg, "// Zeta config file for CUDA device %d (compute capability %d.%d, %d SMs)\n", opencl_device_id,
-          major, minor, sms);
+  fprintf(cfg, "// Zeta config file for %s\n", note ? note : "a CUDA device");
   fprintf(cfg, "################################################################################\n");
-  fprintf(cfg, "threadsX: %d;\n", best_w);
+  fprintf(cfg, "threadsX: %" PRIu64 ";\n", workers);
   fprintf(cfg, "threadsY: %d;\n", 1);
-  fprintf(cfg, "nodes_per_second: %" PRIu64 ";\n", best_nps);
-  fprintf(cfg, "tt1_memory: %" PRIu64 "; // in MB\n", t1);
-  fprintf(cfg, "tt2_memory: %d; // in MB\n", 0);
+  fprintf(cfg, "nodes_per_second: %" PRIu64 ";\n", nps);
+  fprintf(cfg, "tt1_memory: %" PRIu64 "; // in MB\n", tt1_mb);
+  fprintf(cfg, "tt2_memory: %" PRIu64 "; // in MB\n", tt2_mb);
   fprintf(cfg, "opencl_platform_id: %d;\n", 0);
-  fprintf(cfg, "opencl_device_id: %d;\n", opencl_device_id);
+  fprintf(cfg, "opencl_device_id: %d;\n", device);
   fprintf(cfg, "opencl_gpugen: %d;\n", 0);
   fprintf(cfg, "################################################################################\n");
   fprintf(cfg, "# threadsX           // search workers (threadsX x threadsY)\n");
@@ -214,7 +226,5 @@ clrun_bool cl_guess_config(clrun_bool extreme) {
   fprintf(cfg, "# tt2_memory         // MB of device memory for the ABDADA hash table\n");
   fprintf(cfg, "# opencl_device_id   // CUDA device ordinal\n");
   fprintf(cfg, "################################################################################\n");
-  fclose(cfg);
-  printf("#> ### config.txt written: %d workers, %.3f s to depth %d ###\n", best_w, best_s, depth);
-  return 1;
+  return fclose(cfg) == 0 ? 1 : 0;
 }
