@@ -376,9 +376,10 @@ def search_batch_block(z, local, rank, args):
     scores = d_sc.cpu().numpy().copy()
     z.search_set_launch_form(0)
     z.search_set_helpers(0)
-    z.release()
     total_s = sum(ms) / 1e3
     nps = nodes / total_s
+    roofline = _node_roofline(z, nps, "ops_per_search_node", "k_search_warp" if s_form == 3 else "k_search_pure")
+    z.release()
     cpu, vals = (None, None) if args.no_cpu else oracle_search_sample(boards, stm, depth)
     if vals is not None and list(scores[:len(vals)]) != [int(v) for v in vals]:
         raise SystemExit("batched search root scores differ from the oracle's")
@@ -392,7 +393,7 @@ def search_batch_block(z, local, rank, args):
                    "helper_cap": s_helpers, "tt": "1 GiB, 16-byte entries, cleared every step",
                    "l2": "the 1 GiB table and 2.4 G node visits per step exceed L2"},
         "nodes_per_s": round(nps, 1), "nodes_per_step": nodes // steps,
-        "roofline": _node_roofline(z, nps, "ops_per_search_node", "k_search_warp"),
+        "roofline": roofline,
         "oracle_cpu": cpu, "scores_checked_against_oracle": 0 if vals is None else len(vals),
         "clocks": clocks.summary(), "gpu_launches": steps * 3,
     }
@@ -405,7 +406,7 @@ def learned_ab_block(z, local, rank, args):
     identical, time to depth and nodes are compared."""
     from zeta_gb300 import learn
     z.init(local, 1024, 0)
-    boards, stm = _search_arrays(z, rank, args.ab_n or 256)
+    boards, stm = _search_arrays(z, rank, args.ab_n or 512)
     if not learn.load(z):
         z.release()
         return {"unavailable": "no trained network (zeta_gb300/models/ordering_params.npy)", "gpu_launches": 0}
@@ -850,8 +851,8 @@ def main():
     ap.add_argument("--no-search", action="store_true",
                     help="default workload: leave out the batched-search and learned-ordering blocks")
     ap.add_argument("--ab-n", type=int, default=0,
-                    help="learned-ordering A/B: positions (default: 256 in the default line, 1024 with "
-                         "--workload learned_ab)")
+                    help="learned-ordering A/B: positions (default: the first 512 in the default line, "
+                         "all 1024 with --workload learned_ab)")
     ap.add_argument("--ab-depth", type=int, default=8, help="learned-ordering A/B: iterative-deepening depth")
     ap.add_argument("--ab-pairs", type=int, default=3, help="learned-ordering A/B: interleaved plain/learned pairs")
     ap.add_argument("--workload", choices=["perft_batch", "search_batch", "learned_ab", "gemm", "engine", "smp"],

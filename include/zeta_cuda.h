@@ -271,8 +271,10 @@ int zeta_int_peak(double *tops);
 /* Move generation on the device (test and tooling entry): legal moves of
  * n positions, max 256 each, in the reference packing; counts[i] moves
  * for board i.  flags bit 0 keeps captures only; bits 1-2 pick the device
- * generator: 0 the perft generator, 1 the search kernels'.  Both give the
- * same set; the order within a list differs.  Host buffers. */
+ * generator: 0 the perft generator, 1 the search kernels' (one thread per
+ * position), 2 the warp-cooperative search's (one warp per position; the
+ * same list as 1, in the same order).  All give the same set; the order
+ * within a list differs between 0 and the others.  Host buffers. */
 int zeta_genmoves_batch(const uint64_t *boards, const uint8_t *stm, int n, int flags, uint32_t *moves,
                         int32_t *counts);
 /* Static evaluation on the device (test and tooling entry): the reference

@@ -16,7 +16,9 @@
  *     every child from scratch (compute_hash), and compute_hash equals the
  *     oracle's zo_computehash;
  *   - the device evaluation source (eval.cuh) equals the oracle's
- *     zo_eval_white.
+ *     zo_eval_white, and its incremental form (piece terms of the parent
+ *     plus the move's change, plus the structure terms) equals it on every
+ *     child.
  * Linked with the oracle (oracle/zeta_oracle.c) as the checker.
  * Arguments: b0:p1:p2:p3:cr:stm:depth per root.  Prints one line per
  * root; exit status 1 on any disagreement.
@@ -97,6 +99,11 @@ static void walk(const Pos &p, int stm, int depth) {
       g_bad++;
     }
   }
+  const int psum = eval_piece_sum(p, kEvalHost);
+  if (psum + eval_structure(p) != eval_white(p, kEvalHost)) {
+    if (g_bad < 5) printf("piece terms + structure differ from the evaluation\n");
+    g_bad++;
+  }
   if (depth == 0) return;
   Move list[256];
   const int k = gen_legal(p, stm, false, list);
@@ -104,6 +111,10 @@ static void walk(const Pos &p, int stm, int depth) {
   for (int i = 0; i < k; i++) {
     Pos q = p;
     play(q, list[i], false);
+    if (psum + piece_sum_delta(list[i], kEvalHost) != eval_piece_sum(q, kEvalHost)) {
+      if (g_bad < 5) printf("incremental piece terms differ after move %08x\n", list[i]);
+      g_bad++;
+    }
     const u64 inc = th ^ 1ULL ^ cr_keys(p.cr) ^ cr_keys(q.cr) ^ piece_delta(list[i]);
     if (inc != compute_hash(q, stm ^ 1)) {
       if (g_bad < 5) printf("incremental hash differs after move %08x\n", list[i]);

@@ -130,10 +130,12 @@ def test_batch_workload_sample_vs_reference_sum_of_children(zeta_device):
         assert int(sub.sum()) == int(whole[i])
 
 
-@pytest.mark.parametrize("generator", [0, 1])
+@pytest.mark.parametrize("generator", [0, 1, 2])
 def test_genmoves_matches_oracle(zeta_device, generator):
-    """Each device generator (perft, search kernels) gives the oracle's
-    legal set, move for move in the reference packing."""
+    """Each device generator (perft, search kernels, warp-cooperative
+    search) gives the oracle's legal set, move for move in the reference
+    packing; the warp generator gives the search kernels' list in the same
+    order."""
     z = zeta_device
     boards, stm, _ = ol.make_positions(0xD00D, 400, min_plies=1, max_plies=200)
     special = [ol.setboard(f) for f in (
@@ -154,6 +156,10 @@ def test_genmoves_matches_oracle(zeta_device, generator):
         lists = z.genmoves_batch(boards, stm, qs=qs, generator=generator)
         for i in range(len(stm)):
             assert sorted(lists[i].tolist()) == sorted(ol.genmoves(boards[i], stm[i], qs)), (generator, qs, i)
+        if generator == 2:
+            serial = z.genmoves_batch(boards, stm, qs=qs, generator=1)
+            for i in range(len(stm)):
+                assert lists[i].tolist() == serial[i].tolist(), (qs, i)
 
 
 def test_device_positions_match_oracle_generator(zeta_device):

@@ -157,6 +157,8 @@ void mlp_free();
 /* engine.cu: the full-engine search */
 int engine_clear(cudaStream_t s);
 void engine_free();
+int warp_genmoves_launch(const uint64_t *d_boards, const uint8_t *d_stm, int n, int qs, uint32_t *d_moves,
+                         int32_t *d_counts, cudaStream_t s);
 int genmoves_launch(const uint64_t *d_boards, const uint8_t *d_stm, int n, int flags, uint32_t *d_moves,
                     int32_t *d_counts, cudaStream_t stream);
 

@@ -100,4 +100,57 @@ ZHD int eval_white(const Pos &p, const EvalTables &T) {
   return s;
 }
 
+/* ---------------- incremental form ----------------
+ * eval_white is the piece terms (a sum over pieces) plus the pawn-structure
+ * and bishop-pair terms.  The piece terms of a child therefore equal its
+ * parent's plus the change the move makes -- the mover leaves its square,
+ * the moved (or promoted) piece arrives, a captured piece and a castling
+ * rook's old square drop out, the rook's new square comes in -- so a leaf
+ * is scored without the loop over its pieces.  Exact: every term is an
+ * integer and the sum does not depend on its order. */
+
+/* one piece's term in eval_pieces, signed from white's view */
+ZHD int piece_term(int pc, int sq, const EvalTables &T) {
+  const int t = pc >> 1;
+  const bool black = pc & 1;
+  const int v = black ? sq : (sq ^ 56);
+  const int s = 10 + T.value[t] + T.pst[t][v] + T.control[v];
+  return black ? -s : s;
+}
+
+/* the piece terms of eval_white */
+ZHD int eval_piece_sum(const Pos &p, const EvalTables &T) {
+  const u64 occ = p.p1 | p.p2 | p.p3;
+  return eval_pieces(p, occ ^ p.b0, false, T) - eval_pieces(p, p.b0, true, T);
+}
+
+/* the rest of eval_white: pawn structure and bishop pair */
+ZHD int eval_structure(const Pos &p) {
+  const u64 occ = p.p1 | p.p2 | p.p3;
+  const u64 black = p.b0, white = occ ^ p.b0;
+  const u64 pawns = p.p1 & ~p.p2 & ~p.p3;
+  int s = eval_pawns_white(pawns & white, black) - eval_pawns_black(pawns & black, white);
+  const u64 bishops = p.p3 & ~p.p1 & ~p.p2;
+  if (popc(black & bishops) == 2) s -= 25;
+  if (popc(white & bishops) == 2) s += 25;
+  return s;
+}
+
+/* eval_piece_sum(child) - eval_piece_sum(parent) for a real move m (not the
+ * null move), as play() moves the pieces */
+ZHD int piece_sum_delta(Move m, const EvalTables &T) {
+  const int f = m_from(m), t = m_to(m), c = m_cpt(m), pf = m_pfrom(m), pt = m_pto(m), pc = m_pcpt(m);
+  int d = piece_term(pt, t, T) - piece_term(pf, f, T);
+  if (pc >> 1) d -= piece_term(pc, c, T);
+  if ((pf >> 1) == KING && f - t == 2) {
+    const int rook = (ROOK << 1) | (pf & 1);
+    d += piece_term(rook, t + 1, T) - piece_term(rook, f - 4, T);
+  }
+  if ((pf >> 1) == KING && t - f == 2) {
+    const int rook = (ROOK << 1) | (pf & 1);
+    d += piece_term(rook, t - 1, T) - piece_term(rook, f + 3, T);
+  }
+  return d;
+}
+
 }  // namespace zeta

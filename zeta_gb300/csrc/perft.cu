@@ -541,7 +541,8 @@ int perft_run(const uint64_t *d_boards, const uint8_t *d_stm, const uint8_t *d_d
 int genmoves_launch(const uint64_t *d_boards, const uint8_t *d_stm, int n, int flags, uint32_t *d_moves,
                     int32_t *d_counts, cudaStream_t s) {
   const int qs = flags & 1, gen = (flags >> 1) & 3;
-  if (gen > 1) return set_error(ZETA_ERR_ARG, "genmoves: unknown generator");
+  if (gen == 2) return warp_genmoves_launch(d_boards, d_stm, n, qs, d_moves, d_counts, s);
+  if (gen > 2) return set_error(ZETA_ERR_ARG, "genmoves: unknown generator");
   k_genmoves<<<(n + 127) / 128, 128, 0, s>>>(d_boards, d_stm, n, qs, gen, d_moves, d_counts);
   ZCHECK(cudaGetLastError());
   ZCHECK(cudaStreamSynchronize(s));

@@ -495,6 +495,7 @@ struct LeafBatch {
   Pos pos;
   int n, ply, beta;
   uint32_t stm;
+  int psum; /* eval_piece_sum of pos: each leaf adds its move's change */
   Move moves[kMaxMoves];
 };
 
@@ -522,14 +523,52 @@ constexpr unsigned kFull = 0xFFFFFFFFu;
  * out-of-line copy each: the piece sets, the enemy attack map and the 23
  * emitter sets of (pos, stm) -- returns the number of legal moves -- and
  * move j of the list. */
-__device__ __noinline__ int w_plan(const Pos &pos, int stm, u64 *set, bool *chk, int *sqep, Sets *sets) {
+__device__ __noinline__ int w_plan(const Pos &pos, int stm, bool qs, u64 *set, bool *chk, int *sqep, Sets *sets) {
   const Sets s = make_sets(pos, stm);
   *sets = s;
-  return gen_plan_rolled(pos, s, enemy_attacks_rolled(s, stm), stm, false, set, chk, sqep);
+  return gen_plan_rolled(pos, s, enemy_attacks_rolled(s, stm), stm, qs, set, chk, sqep);
 }
 __device__ __noinline__ Move w_move_at(const Pos &p, const Sets &s, int stm, const u64 *set, const uint8_t *off,
                                        int sqep, int j) {
   return gen_move_at_rolled(p, s, stm, set, off, sqep, j);
+}
+
+/* the legal moves of n positions, one warp each, with the warp-cooperative
+ * search's generator -- the same plan and per-lane decode as warp_plan and
+ * warp_gen_order (test entry: the list must equal gen_engine's, in the
+ * same order) */
+__global__ void k_genmoves_warp(const uint64_t *__restrict__ boards, const uint8_t *__restrict__ stm, int n, int qs,
+                                uint32_t *__restrict__ moves, int32_t *__restrict__ counts) {
+  __shared__ u64 wset[4][kEmitters];
+  __shared__ uint8_t woff[4][kEmitters + 1];
+  const int lane = threadIdx.x & 31, wi = threadIdx.x >> 5;
+  const int i = blockIdx.x * 4 + wi;
+  if (i >= n) return; /* whole warps */
+  const uint64_t *b = boards + 7 * (size_t)i;
+  Pos p;
+  p.b0 = b[0];
+  p.p1 = b[1];
+  p.p2 = b[2];
+  p.p3 = b[3];
+  p.cr = b[4];
+  const int side = stm[i] & 1;
+  Sets s;
+  bool chk;
+  int sqep;
+  int cnt = w_plan(p, side, qs != 0, wset[wi], &chk, &sqep, &s);
+  __syncwarp();
+  int c = lane < kEmitters ? popc(wset[wi][lane]) : 0;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xFFFFFFFFu, c, o);
+    if (lane >= o) c += y;
+  }
+  if (lane < kEmitters) woff[wi][lane + 1] = (uint8_t)min(c, 255);
+  if (lane == 0) woff[wi][0] = 0;
+  __syncwarp();
+  cnt = cnt < 256 ? cnt : 256;
+  for (int j = lane; j < cnt; j += 32) moves[(size_t)i * 256 + j] = w_move_at(p, s, side, wset[wi], woff[wi], sqep, j);
+  if (lane == 0) counts[i] = cnt;
 }
 
 /* whether the side to move has a legal move, and whether it is in check:
@@ -544,15 +583,16 @@ __device__ __noinline__ bool w_has_move(const Pos &p, int stm, bool *chk) {
   u64 set[kEmitters];
   int sqep;
   Sets s;
-  const int n = w_plan(p, stm, set, chk, &sqep, &s);
+  const int n = w_plan(p, stm, false, set, chk, &sqep, &s);
   return n > 0;
 }
 
-/* value of a node with no depth left, from the side to move */
-__device__ __forceinline__ int leaf_value_w(const Pos &p, int stm, int ply, const EvalTables *T) {
+/* value of a node with no depth left, from the side to move; psum: its
+ * piece terms (eval.cuh, incremental form) */
+__device__ __forceinline__ int leaf_value_w(const Pos &p, int stm, int ply, int psum) {
   bool chk;
   if (!w_has_move(p, stm, &chk)) return chk ? -kSearchInf + ply : 0;
-  const int e = s_eval(p, T);
+  const int e = psum + eval_structure(p);
   return stm ? -e : e;
 }
 
@@ -579,7 +619,7 @@ struct WFrame {
  * resource. */
 __device__ __noinline__ int warp_plan(WarpGen &G, const Pos &pos, int stm, Sets &s, int &sqep, int lane) {
   bool chk = false;
-  int n = w_plan(pos, stm, G.set, &chk, &sqep, &s);
+  int n = w_plan(pos, stm, false, G.set, &chk, &sqep, &s);
   __syncwarp();
   int c = lane < kEmitters ? popc(G.set[lane]) : 0;
 #pragma unroll
@@ -642,13 +682,25 @@ __device__ __forceinline__ int warp_gen_order(WarpGen &G, const EvalTables &T, i
 
 /* All lanes: the legal moves of B.pos into B.moves, captures and
  * promotions first when they take more than one scoring round (each group
- * in generation order). */
-__device__ __forceinline__ int warp_gen_batch(WarpGen &G, LeafBatch &B, int lane) {
+ * in generation order), and the piece terms of B.pos (one piece per lane). */
+__device__ __forceinline__ int warp_gen_batch(WarpGen &G, LeafBatch &B, const EvalTables &T, int lane) {
   Sets s;
   int sqep = 0;
   const Pos pos = B.pos;
   const int stm = B.stm;
   const int n = warp_plan(G, pos, stm, s, sqep, lane);
+  {
+    const u64 occ = pos.p1 | pos.p2 | pos.p3;
+    const int npc = popc(occ);
+    int ps = 0;
+    for (int k = lane; k < npc; k += 32) {
+      const int sq = select_bit(occ, k);
+      ps += piece_term(piece_at(pos, sq), sq, T);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) ps += __shfl_xor_sync(kFull, ps, o);
+    if (lane == 0) B.psum = ps;
+  }
   if (n <= 32) {
     if (lane < n) B.moves[lane] = w_move_at(pos, s, stm, G.set, G.off, sqep, lane);
   } else {
@@ -1074,15 +1126,16 @@ __global__ void __launch_bounds__(TPB, 4) k_search_warp(const uint64_t *__restri
       continue;
     }
     /* cmd 3: generate the batch node's moves, then score its children */
-    const int n = warp_gen_batch(G, B, lane);
+    const int n = warp_gen_batch(G, B, sT, lane);
     const int beta = B.beta;
     int best = -kSearchInf - 1, bi = 0, scored = 0;
     for (int base = 0; base < n; base += 32) {
       const int i = base + lane;
       if (i < n) {
         Pos c = B.pos;
-        play(c, B.moves[i], false);
-        const int v = -leaf_value_w(c, B.stm ^ 1, B.ply + 1, &sT);
+        const Move m = B.moves[i];
+        play(c, m, false);
+        const int v = -leaf_value_w(c, B.stm ^ 1, B.ply + 1, B.psum + piece_sum_delta(m, sT));
         if (v > best) {
           best = v;
           bi = i;
@@ -1159,6 +1212,14 @@ static int search_buffers(int n) {
     ZCHECK(cudaMalloc(&c.s_tt, c.s_tt_entries * sizeof(TTEntry)));
     ZCHECK(cudaMemset(c.s_tt, 0, c.s_tt_entries * sizeof(TTEntry)));
   }
+  return ZETA_OK;
+}
+
+int warp_genmoves_launch(const uint64_t *d_boards, const uint8_t *d_stm, int n, int qs, uint32_t *d_moves,
+                         int32_t *d_counts, cudaStream_t s) {
+  k_genmoves_warp<<<(n + 3) / 4, 128, 0, s>>>(d_boards, d_stm, n, qs, d_moves, d_counts);
+  ZCHECK(cudaGetLastError());
+  ZCHECK(cudaStreamSynchronize(s));
   return ZETA_OK;
 }
 
