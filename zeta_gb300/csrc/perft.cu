@@ -387,6 +387,22 @@ int perft_ensure_arena(uint64_t tasks_cap) {
 int perft_run(const uint64_t *d_boards, const uint8_t *d_stm, const uint8_t *d_depth, int n, uint64_t *d_leaves,
               cudaStream_t s);
 
+/* Per-thread stack for kernel k.  Every perft kernel keeps a 256-move list
+ * on its stack and the register-capped variants spill next to it (1024 to
+ * 1152 bytes; the 64-register variants, which are not built, needed 1264),
+ * above CUDA's 1 KB default.  The driver grows the stack when a kernel is
+ * launched directly; this path replays its launches from a CUDA graph, so
+ * the stack is sized here, before the sequence is captured, instead of
+ * relying on that. */
+static int ensure_stack(const void *k) {
+  cudaFuncAttributes fa;
+  ZCHECK(cudaFuncGetAttributes(&fa, k));
+  size_t cur = 0;
+  ZCHECK(cudaDeviceGetLimit(&cur, cudaLimitStackSize));
+  if (fa.localSizeBytes > cur) ZCHECK(cudaDeviceSetLimit(cudaLimitStackSize, fa.localSizeBytes));
+  return ZETA_OK;
+}
+
 /* grid of the work-stealing kernel, cursors and per-block scratch */
 static int ws_geometry(int &blocks, int &tpb, WsKernel &k) {
   Context &c = ctx();
@@ -395,6 +411,9 @@ static int ws_geometry(int &blocks, int &tpb, WsKernel &k) {
   if (!k)
     return set_error(ZETA_ERR_ARG, "no perft kernel variant for %d threads x %d blocks per SM", tpb,
                      c.pcfg.blocks_per_sm);
+  int rc = ensure_stack((const void *)k);
+  if (!rc) rc = ensure_stack((const void *)k_split);
+  if (rc) return rc;
   int bps = 0;
   ZCHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k, tpb, 0));
   if (bps < 1) bps = 1;

@@ -26,13 +26,14 @@ MODEL = os.path.join(HERE, "models", "ordering_params.npy")
 TRAIN_SEED = 0x5A17A0000000004   # disjoint from the evaluation workloads' seeds
 
 
-def make_dataset(z, n: int, label_depth: int, seed: int = TRAIN_SEED, workers: int = 8, helpers: int = 32):
+def make_dataset(z, n: int, label_depth: int, seed: int = TRAIN_SEED, workers: int = 2, helpers: int = 64,
+                 chunk: int = 1024):
     """n positions (10-60 random plies) and the plain search's best move at
-    label_depth, 8192 positions per launch (8 workers each, finished workers
-    help up to 32 per position: the fastest setting measured for labelling)."""
+    label_depth, `chunk` positions per launch with `workers` ABDADA workers
+    each and finished workers helping up to `helpers` per position (one warp
+    per worker: the warp-cooperative form, the fastest measured)."""
     boards, stm, _ = z.make_positions(seed, n, 10, 60, 0, 0, 0)
     best = np.zeros(n, dtype=np.uint32)
-    chunk = 8192
     z.search_set_helpers(helpers)
     try:
         for off in range(0, n, chunk):
