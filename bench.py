@@ -664,9 +664,9 @@ def run_smp(args):
     import zeta_gb300 as z
     world, rank, local = dist_env()
     torch.cuda.set_device(local)
-    z.init(local, 2048, args.tt2_mb)
+    z.init(local, args.tt1_mb, args.tt2_mb)
     depth = args.depth or 12
-    wlist = [args.workers] if args.workers else [64, 128, 192, 256, 384, 512, 1024]
+    wlist = [args.workers] if args.workers else [int(x) for x in args.smp_workers.split(",")]
     b = z.STARTPOS
 
     def run(W):
@@ -706,8 +706,8 @@ def run_smp(args):
             "vs_baseline": round(best["seconds"] / 4.871, 4) if depth == 12 else None,
             "baseline": "4.871 s: Titan RTX, 128 work-groups, version 099k (results.txt:37)",
             "dtype": "int32", "data": "the initial position",
-            "config": {"workload": f"startpos iterative deepening 1..{depth}, 2 GB TT1 + {args.tt2_mb} MB TT2, "
-                                   "fresh tables",
+            "config": {"workload": f"startpos iterative deepening 1..{depth}, {args.tt1_mb} MB TT1 + {args.tt2_mb} MB "
+                                   "TT2, fresh tables",
                        "workers": best["workers"], "statistic": f"median of {len(reps)} runs",
                        "runs_s": [r["seconds"] for r in reps]},
             "nodes_per_s": best["nps"],
@@ -862,6 +862,8 @@ def main():
     ap.add_argument("--helpers", type=int, default=0, help="helper cap: max workers per position (0 = none)")
     ap.add_argument("--form", type=int, default=0,
                     help="search_batch launch form with --workers: 0 auto, 1 dense, 2 sparse, 3 warp-cooperative")
+    ap.add_argument("--tt1-mb", type=int, default=2048, help="smp: transposition table size")
+    ap.add_argument("--smp-workers", default="64,128,192,256,384,512,1024", help="smp: worker counts of the sweep")
     ap.add_argument("--tt2-mb", type=int, default=0,
                     help="smp: ABDADA table size (0 = no TT2: helpers randomise their move order instead)")
     args = ap.parse_args()

@@ -196,6 +196,26 @@ def test_zeta_st_one_second_moves_in_time(tmp_path):
 
 
 @pytest.mark.gpu
+def test_zeta_benchfile_sweeps_workers_over_a_position_list(tmp_path):
+    """benchfile (the harness of the reference's benchkaufmann /
+    benchhyatt24, src/xboard.c:975-1428): a worker sweep per position, one
+    results.txt table each, then the table of the summed times."""
+    fens = tmp_path / "positions.epd"
+    fens.write_text("r3k2r/p1ppqpb1/bn2pnp1/3PN3/1p2P3/2N2Q1p/PPPBBPPP/R3K2R w KQkq -\n"
+                    "# a comment line\n"
+                    "8/2p5/3p4/KP5r/1R3p1k/8/4P1P1/8 w - -\n")
+    r = subprocess.run([ZETA], input=f"sd 4\nbenchfile {fens} 2\nquit\n", capture_output=True, text=True,
+                       timeout=600, cwd=tmp_path)
+    assert r.returncode == 0, r.stderr
+    out = r.stdout
+    assert "### setting up board 2: ###" in out and "### all 2 positions: ###" in out
+    rows = [l.split() for l in out.splitlines() if l.startswith("### 1\t") or l.startswith("### 2\t")]
+    assert len(rows) == 6  # workers 1 and 2, for two positions and the sum
+    total = out.split("### all 2 positions: ###")[1]
+    assert total.count("\n### 1\t") == 1 and total.count("\n### 2\t") == 1
+
+
+@pytest.mark.gpu
 def test_zeta_xboard_session_plays_a_legal_move():
     session = "xboard\nprotover 2\nnew\nsd 4\nusermove e2e4\nquit\n"
     r = subprocess.run([ZETA], input=session, capture_output=True, text=True, timeout=600, cwd=ROOT)

@@ -97,28 +97,22 @@ void perft(Bitboard *board, int stm, int depth) {
   for (uint64_t i = 0; i < totalWorkUnits; i++) ABNODECOUNT += COUNTERS[i * 64 + 1];
 }
 
-/* Worker-scaling benchmark (the reference's `benchsmp`, src/xboard.c:822-974):
- * the same iterative-deepening search to `depth` with 1, 2, 4, ... workers
- * up to max_workers, each run from fresh tables, then one table of nodes
- * per second, time-to-depth and the speedups over 1 worker and over the
- * previous worker count, in the reference's results.txt layout. */
-void benchsmp(Bitboard *board, int stm, int depth, uint64_t max_workers) {
-  enum { kMaxRuns = 40 };
-  double secs[kMaxRuns];
-  uint64_t nps[kMaxRuns], workers[kMaxRuns];
+/* One worker sweep: the iterative-deepening search of `board` to `depth`
+ * with 1, 2, 4, ... workers up to max_workers, each run from fresh tables;
+ * times (s), node rates and worker counts into the arrays (kMaxRuns long),
+ * returns the number of runs. */
+enum { kMaxRuns = 40 };
+static int worker_sweep(Bitboard *board, int stm, int depth, uint64_t max_workers, const char *name, double *secs,
+                        uint64_t *nps, uint64_t *workers) {
   int runs = 0;
-  const uint64_t saved = totalWorkUnits, saved_nodes = MaxNodes;
-  const double saved_time = MaxTime;
-  MaxNodes = 0; /* a depth-limited benchmark: no node or time budget */
-  MaxTime = 1e15;
   if (max_workers < 1) max_workers = 1;
   for (uint64_t w = 1; runs < kMaxRuns;) {
-    printf("### doing inits for benchsmp depth %d: ###\n", depth);
+    printf("### doing inits for %s depth %d: ###\n", name, depth);
     totalWorkUnits = w;
     engine_free();
     if (!engine_alloc()) die();
     if (!cl_release_device() || !cl_init_device("alphabeta_gpu")) die(); /* fresh tables */
-    printf("### computing benchsmp depth %d: ###\n", depth);
+    printf("### computing %s depth %d: ###\n", name, depth);
     printf("### work-groups: %" PRIu64 " ###\n", w);
     double t0 = get_time_ms();
     rootsearch(board, stm, depth);
@@ -130,6 +124,11 @@ void benchsmp(Bitboard *board, int stm, int depth, uint64_t max_workers) {
     if (w >= max_workers) break;
     w = w * 2 > max_workers ? max_workers : w * 2;
   }
+  return runs;
+}
+
+/* the results.txt table (src/xboard.c:923-944) */
+static void scaling_table(int runs, const double *secs, const uint64_t *nps, const uint64_t *workers) {
   printf("### workers\t#nps\t\t#nps speedup\t#time in s\t#ttd speedup \t#relative ttd speedup ###\n");
   for (int i = 0; i < runs; i++) {
     const double ns = nps[0] ? (double)nps[i] / (double)nps[0] : 0.0;
@@ -139,13 +138,87 @@ void benchsmp(Bitboard *board, int stm, int depth, uint64_t max_workers) {
       fprintf(LogFile, "### %" PRIu64 "\t\t%" PRIu64 "\t\t%lf\t%lf\t%lf\t%lf \n", workers[i], nps[i], ns, secs[i],
               ttd, rel);
   }
-  totalWorkUnits = saved;
-  MaxNodes = saved_nodes;
-  MaxTime = saved_time;
+}
+
+/* a depth-limited benchmark runs without node or time budget; the caller's
+ * budgets, worker count and tables come back afterwards */
+static uint64_t g_saved_workers, g_saved_nodes;
+static double g_saved_time;
+static void bench_begin(void) {
+  g_saved_workers = totalWorkUnits;
+  g_saved_nodes = MaxNodes;
+  g_saved_time = MaxTime;
+  MaxNodes = 0;
+  MaxTime = 1e15;
+}
+static void bench_end(void) {
+  totalWorkUnits = g_saved_workers;
+  MaxNodes = g_saved_nodes;
+  MaxTime = g_saved_time;
   engine_free();
   if (!engine_alloc()) die();
   if (!cl_release_device() || !cl_init_device("alphabeta_gpu")) die();
   fflush(stdout);
+}
+
+/* Worker-scaling benchmark (the reference's `benchsmp`, src/xboard.c:822-974):
+ * the same iterative-deepening search to `depth` with 1, 2, 4, ... workers
+ * up to max_workers, each run from fresh tables, then one table of nodes
+ * per second, time-to-depth and the speedups over 1 worker and over the
+ * previous worker count, in the reference's results.txt layout. */
+void benchsmp(Bitboard *board, int stm, int depth, uint64_t max_workers) {
+  double secs[kMaxRuns];
+  uint64_t nps[kMaxRuns], workers[kMaxRuns];
+  bench_begin();
+  const int runs = worker_sweep(board, stm, depth, max_workers, "benchsmp", secs, nps, workers);
+  scaling_table(runs, secs, nps, workers);
+  bench_end();
+}
+
+/* The position-list benchmarks (the reference's `benchkaufmann` and
+ * `benchhyatt24`, src/xboard.c:975-1200, 1203-1428): the worker sweep of
+ * benchsmp on every position of a list, one table per position, then the
+ * table of the times summed over the positions.  The reference embeds its
+ * two lists (src/xboard.c:986-1012, 1214-1240); here the list is a file
+ * of FEN lines, so any list -- those two included -- can be run. */
+int benchfile(const char *path, int depth, uint64_t max_workers) {
+  FILE *f = fopen(path, "r");
+  if (!f) {
+    printf("Error (cannot open %s): benchfile\n", path);
+    return 0;
+  }
+  double secs[kMaxRuns], total[kMaxRuns] = {0};
+  uint64_t nps[kMaxRuns], workers[kMaxRuns], nodes[kMaxRuns] = {0};
+  int runs = 0, posi = 0;
+  char line[1024];
+  bench_begin();
+  while (fgets(line, sizeof line, f)) {
+    Bitboard b[7];
+    int side, full;
+    if (strlen(line) < 8 || line[0] == '#') continue;
+    if (!board_setfen(b, &side, &full, line)) {
+      printf("# Error (in setting fen position): %s", line);
+      continue;
+    }
+    posi++;
+    printf("#\n#\n### setting up board %d: ###\n", posi);
+    memset(HashHistory, 0, sizeof HashHistory);
+    HashHistory[0] = b[QBBHASH];
+    runs = worker_sweep(b, side, depth, max_workers, "benchfile", secs, nps, workers);
+    scaling_table(runs, secs, nps, workers);
+    for (int i = 0; i < runs; i++) {
+      total[i] += secs[i];
+      nodes[i] += (uint64_t)((double)nps[i] * secs[i]);
+    }
+  }
+  fclose(f);
+  if (posi > 0) {
+    printf("#\n### all %d positions: ###\n", posi);
+    for (int i = 0; i < runs; i++) nps[i] = (uint64_t)((double)nodes[i] / total[i]);
+    scaling_table(runs, total, nps, workers);
+  }
+  bench_end();
+  return posi;
 }
 
 /* The 14 known-answer tests of the reference's selftest (src/test.c:43-73). */

@@ -50,6 +50,7 @@ void perft(Bitboard *board, int stm, int depth);             /* src/search.c:225
 Move rootsearch(Bitboard *board, int stm, int depth);        /* src/search.c:35-223 */
 int selftest(void);                                          /* src/test.c:36-169 */
 void benchsmp(Bitboard *board, int stm, int depth, uint64_t max_workers); /* src/xboard.c:822-974 */
+int benchfile(const char *path, int depth, uint64_t max_workers); /* src/xboard.c:975-1428, list from a file */
 void xboard(void);                                           /* src/xboard.c:44-1499 */
 
 #endif

@@ -166,6 +166,17 @@ void xboard(void) {
       /* benchsmp [max workers]: worker scaling of the search to depth sd */
       uint64_t maxw = strtoull(arg, NULL, 10);
       benchsmp(BOARD, STM, SD, maxw ? maxw : totalWorkUnits);
+    } else if (!strcmp(cmd, "benchfile") && !xboard_mode) {
+      /* benchfile <file of FEN lines> [max workers]: benchsmp on every
+       * position, then the summed table (benchkaufmann / benchhyatt24) */
+      char path[512] = {0};
+      unsigned long long maxw = 0;
+      if (sscanf(arg, "%511s %llu", path, &maxw) < 1) {
+        printf("Error (usage: benchfile <file> [max workers])\n");
+      } else {
+        benchfile(path, SD, maxw ? (uint64_t)maxw : totalWorkUnits);
+        HashHistory[0] = BOARD[QBBHASH];
+      }
     } else if (!strcmp(cmd, "print") && !xboard_mode) {
       char fen[256];
       board_print(BOARD, STM);
@@ -174,6 +185,7 @@ void xboard(void) {
     } else if (!strcmp(cmd, "help") && !xboard_mode) {
       printf("# commands: new, setboard <fen>, go, usermove <move>, force, sd <depth>, st <seconds>,\n"
              "# level <moves> <minutes> <increment>, time <centiseconds>, perft <depth>,\n"
+             "# benchfile <file of FENs> [max workers],\n"
              "# benchsmp [max workers], selftest, print, quit (and the xboard protocol)\n");
     } else if (!strcmp(cmd, "accepted") || !strcmp(cmd, "rejected") || !strcmp(cmd, "random") ||
                !strcmp(cmd, "computer") || !strcmp(cmd, "result") || !strcmp(cmd, "hard") ||
