@@ -407,9 +407,10 @@ def learned_ab_block(z, local, rank, args):
     from zeta_gb300 import learn
     z.init(local, 1024, 0)
     boards, stm = _search_arrays(z, rank, args.ab_n or 512)
-    if not learn.load(z):
+    model = args.ab_model or learn.MODEL
+    if not learn.load(z, model):
         z.release()
-        return {"unavailable": "no trained network (zeta_gb300/models/ordering_params.npy)", "gpu_launches": 0}
+        return {"unavailable": f"no trained network ({os.path.relpath(model, ROOT)})", "gpu_launches": 0}
     depth, pairs = args.ab_depth, args.ab_pairs
     _, s_workers, s_helpers = _search_setting()
     z.search_set_helpers(s_helpers)
@@ -435,6 +436,7 @@ def learned_ab_block(z, local, rank, args):
     return {
         "metric": f"time to depth {depth}, learned (BF16 network) vs plain ordering, same root scores",
         "config": {"workload": f"search_batch: {len(stm)} playouts, iterative deepening 1..{depth}",
+                   "model": os.path.relpath(model, ROOT),
                    "form": "automatic (warp-cooperative)", "workers_per_position": s_workers,
                    "helper_cap": s_helpers, "pairs": pairs, "order": "plain then learned, interleaved"},
         "plain": {"ms_median": round(med(0, "ms"), 1), "ms_runs": [round(r["ms"], 1) for r in runs[0]],
@@ -855,6 +857,7 @@ def main():
                          "all 1024 with --workload learned_ab)")
     ap.add_argument("--ab-depth", type=int, default=8, help="learned-ordering A/B: iterative-deepening depth")
     ap.add_argument("--ab-pairs", type=int, default=3, help="learned-ordering A/B: interleaved plain/learned pairs")
+    ap.add_argument("--ab-model", default="", help="learned-ordering A/B: network parameters (default: the committed)")
     ap.add_argument("--workload", choices=["perft_batch", "search_batch", "learned_ab", "gemm", "engine", "smp"],
                     default="perft_batch")
     ap.add_argument("--depth", type=int, default=0, help="search depth (search_batch; default 7)")
