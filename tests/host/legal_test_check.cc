@@ -3,9 +3,10 @@
  * movegen_fast.cuh, tables.cuh) for the CPU tests.  Walks full move trees
  * and checks at every node that
  *   - the quick free-move test (has_free_move, used at pure-search leaves)
- *     never claims a legal move where the exact count (count_legal_ex)
- *     finds none, has_legal_ex equals "count > 0", and all three report
- *     the same in-check flag;
+ *     and its king-step extension (has_quick_move_rolled) never claim a
+ *     legal move where the exact count (count_legal_ex) finds none,
+ *     has_legal_ex equals "count > 0", and all report the same in-check
+ *     flag;
  *   - the search kernels' generator (gen_engine) gives the perft
  *     generator's (gen_legal) move set, all moves and captures only;
  *   - the warp generator's plan and per-move decode (warpgen.cuh), in
@@ -37,16 +38,22 @@
 
 using namespace zeta;
 
-static unsigned long long g_nodes = 0, g_bad = 0, g_quick = 0;
+static unsigned long long g_nodes = 0, g_bad = 0, g_quick = 0, g_king = 0;
 
 static void walk(const Pos &p, int stm, int depth) {
   bool c1, c2, c3;
   const int n = count_legal_ex(p, stm, c1);
   const bool quick = has_free_move(p, stm, c2);
   {
-    bool cr;
+    bool cr, ck;
     if (has_free_move_rolled(p, stm, cr) != quick || cr != c2) {
       if (g_bad < 5) printf("rolled quick test differs\n");
+      g_bad++;
+    }
+    const bool qk = has_quick_move_rolled(p, stm, ck);
+    g_king += qk && !quick;
+    if ((qk && n == 0) || ck != c1) {
+      if (g_bad < 5) printf("king-step quick test claims a move the count does not find\n");
       g_bad++;
     }
   }
@@ -134,7 +141,8 @@ int main(int argc, char **argv) {
     }
     const Pos p{v[0], v[1], v[2], v[3], v[4]};
     walk(p, (int)v[5], (int)v[6]);
-    printf("root %d: %llu nodes, %llu decided by the quick test, %llu disagreements\n", r, g_nodes, g_quick, g_bad);
+    printf("root %d: %llu nodes, %llu decided by the quick test, %llu more by the king step, %llu disagreements\n", r,
+           g_nodes, g_quick, g_king, g_bad);
   }
   return g_bad != 0;
 }

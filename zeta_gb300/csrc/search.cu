@@ -572,11 +572,13 @@ __global__ void k_genmoves_warp(const uint64_t *__restrict__ boards, const uint8
 }
 
 /* whether the side to move has a legal move, and whether it is in check:
- * the quick free-move test, then the legal-move count of w_plan (the
- * generator's own code, so the leaf test adds no second copy of it) */
+ * the quick free-move and king-step tests, then the legal-move count of
+ * w_plan (the generator's own code, so the leaf test adds no second copy
+ * of it).  The count is needed for well under 1% of the leaves: a warp
+ * whose lanes all decide quickly skips it. */
 __device__ __noinline__ bool w_has_move(const Pos &p, int stm, bool *chk) {
   bool c;
-  if (has_free_move_rolled(p, stm, c)) {
+  if (has_quick_move_rolled(p, stm, c)) {
     *chk = c;
     return true;
   }

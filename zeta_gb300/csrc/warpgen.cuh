@@ -379,6 +379,17 @@ ZE bool has_free_move_rolled(const Pos &p, int stm, bool &in_check) {
   return ((push & empty) | (pawn_attacks(P, stm) & s.them)) != 0;
 }
 
+/* has_free_move_rolled, then a king step: when no other piece proves a
+ * legal move -- always the case in check -- a king step to a square the
+ * enemy does not attack (the attack map made with the king off the board,
+ * so it cannot step back along a checking ray) is one.  true proves a legal
+ * move; false leaves the question to the exact count.  in_check is exact. */
+ZE bool has_quick_move_rolled(const Pos &p, int stm, bool &in_check) {
+  if (has_free_move_rolled(p, stm, in_check)) return true;
+  const Sets s = make_sets(p, stm);
+  return (king_attacks(s.kbb) & ~s.us & ~enemy_attacks_rolled(s, stm)) != 0;
+}
+
 /* gen_decode with the slider's origin from a run-time-direction ray */
 ZE Move gen_decode_rolled(const Pos &p, const Sets &s, int stm, int e, int sq, int sqep) {
   if (e < 8) {
