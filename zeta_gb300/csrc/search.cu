@@ -495,7 +495,7 @@ struct LeafBatch {
   Pos pos;
   int n, ply, beta;
   uint32_t stm;
-  int psum; /* eval_piece_sum of pos: each leaf adds its move's change */
+  int psum; /* eval_piece_sum of pos (carried down the walk): each leaf adds its move's change */
   Move moves[kMaxMoves];
 };
 
@@ -610,6 +610,7 @@ struct WFrame {
   int n, i, iter, searched;
   int depth;
   uint8_t stm, exclusive, deferred, busy;
+  int psum; /* eval_piece_sum of pos (eval.cuh, incremental form) */
   Move moves[kMaxMoves];
 };
 
@@ -684,25 +685,14 @@ __device__ __forceinline__ int warp_gen_order(WarpGen &G, const EvalTables &T, i
 
 /* All lanes: the legal moves of B.pos into B.moves, captures and
  * promotions first when they take more than one scoring round (each group
- * in generation order), and the piece terms of B.pos (one piece per lane). */
-__device__ __forceinline__ int warp_gen_batch(WarpGen &G, LeafBatch &B, const EvalTables &T, int lane) {
+ * in generation order). */
+__device__ __forceinline__ int warp_gen_batch(WarpGen &G, LeafBatch &B, int lane) {
   Sets s;
   int sqep = 0;
   const Pos pos = B.pos;
   const int stm = B.stm;
   const int n = warp_plan(G, pos, stm, s, sqep, lane);
-  {
-    const u64 occ = pos.p1 | pos.p2 | pos.p3;
-    const int npc = popc(occ);
-    int ps = 0;
-    for (int k = lane; k < npc; k += 32) {
-      const int sq = select_bit(occ, k);
-      ps += piece_term(piece_at(pos, sq), sq, T);
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) ps += __shfl_xor_sync(kFull, ps, o);
-    if (lane == 0) B.psum = ps;
-  }
+
   if (n <= 32) {
     if (lane < n) B.moves[lane] = w_move_at(pos, s, stm, G.set, G.off, sqep, lane);
   } else {
@@ -924,6 +914,7 @@ __global__ void __launch_bounds__(TPB, 4) k_search_warp(const uint64_t *__restri
           F[0].pos.p3 = b[3];
           F[0].pos.cr = b[4];
           F[0].th = compute_hash(F[0].pos, stm[p] & 1);
+          F[0].psum = eval_piece_sum(F[0].pos, sT);
           F[0].stm = stm[p] & 1;
           F[0].depth = depth;
           F[0].alpha = -kSearchInf - 1;
@@ -933,6 +924,7 @@ __global__ void __launch_bounds__(TPB, 4) k_search_warp(const uint64_t *__restri
             W.nodes++;
             F[0].key = search_key(F[0].pos, F[0].th);
             B.pos = F[0].pos;
+            B.psum = F[0].psum;
             B.stm = F[0].stm;
             B.ply = 0;
             B.beta = kSearchInf + 1;
@@ -1050,6 +1042,7 @@ __global__ void __launch_bounds__(TPB, 4) k_search_warp(const uint64_t *__restri
             g.pos = f.pos;
             play(g.pos, m, false);
             g.th = f.th ^ 1ULL ^ cr_keys(f.pos.cr) ^ cr_keys(g.pos.cr) ^ piece_delta(m);
+            g.psum = f.psum + piece_sum_delta(m, sT); /* the child's piece terms */
             g.stm = f.stm ^ 1;
             g.depth = f.depth - 1;
             g.alpha = -f.beta;
@@ -1072,6 +1065,7 @@ __global__ void __launch_bounds__(TPB, 4) k_search_warp(const uint64_t *__restri
               }
               if (!hit) {
                 B.pos = g.pos;
+                B.psum = g.psum;
                 B.stm = g.stm;
                 B.ply = ply + 1;
                 B.beta = g.beta;
@@ -1128,7 +1122,7 @@ __global__ void __launch_bounds__(TPB, 4) k_search_warp(const uint64_t *__restri
       continue;
     }
     /* cmd 3: generate the batch node's moves, then score its children */
-    const int n = warp_gen_batch(G, B, sT, lane);
+    const int n = warp_gen_batch(G, B, lane);
     const int beta = B.beta;
     int best = -kSearchInf - 1, bi = 0, scored = 0;
     for (int base = 0; base < n; base += 32) {
