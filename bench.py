@@ -43,10 +43,14 @@ OPS_PER_COUNTED_NODE = None  # filled from profiles/opcount.json when present
 OPS_PER_INTERIOR_NODE = None
 
 
-def _opcounts():
+def _opcounts(tree: str = "startpos_d5"):
+    """Algorithmic int32 operations per bulk-counted and per interior perft
+    node, counted once on the perft generator's own code
+    (zeta_gb300/csrc/opcount.cc): over the initial position's depth-5 tree
+    (the fixed denominator) or over the 64-position workload sample."""
     path = os.path.join(ROOT, "profiles", "opcount.json")
     if os.path.exists(path):
-        d = json.load(open(path))
+        d = json.load(open(path))[tree]
         return d["ops_per_counted_node"], d["ops_per_interior_node"]
     return None, None
 
@@ -177,6 +181,7 @@ def run_ours(args):
     z.init(local, 0, 0)
     from zeta_gb300.autotune import load_tuned
     load_tuned(z)  # the autotuner's launch configuration, when recorded
+    z.perft_set_promotions(args.all_promotions)
     info = z.device_info()
     boards, stm, depth = workload_arrays(z, rank, args.n)
     n = len(depth)
@@ -255,9 +260,12 @@ def run_ours(args):
         int_peak = None
     kernel_avg_ms = sum(kernel_ms) / len(kernel_ms)
     roofline = None
-    if ops_c and int_peak:
+    # the per-node operation counts are those of the queen-only kernel
+    if ops_c and int_peak and not args.all_promotions:
         ops = (counted / args.steps) * ops_c + (interior / args.steps) * ops_i
         achieved = ops / (kernel_avg_ms / 1e3) / 1e12
+        wc, wi = _opcounts("workload_sample")
+        ops_w = (counted / args.steps) * wc + (interior / args.steps) * wi
         traffic = None
         tp = os.path.join(ROOT, "profiles", "perft_ws_traffic.json")
         if os.path.exists(tp):
@@ -265,13 +273,18 @@ def run_ours(args):
         roofline = {"bound": "int32-alu", "achieved": round(achieved, 3), "peak": round(int_peak, 3),
                     "unit": "Tops/s", "frac": round(achieved / int_peak, 4), "traffic": traffic,
                     "peak_source": "measured: int32 LOP3/SHF/IADD3 microbenchmark (zeta_int_peak)",
-                    "kernel": "k_perft_ws"}
-    cpu = None if args.no_cpu else cpu_baseline_sample(boards, stm, depth)
+                    "kernel": "k_perft_ws",
+                    "ops_per_node": {"counted": ops_c, "interior": ops_i,
+                                     "source": "initial position, depth-5 tree (fixed once)"},
+                    "frac_workload_sample_ops": round(ops_w / (kernel_avg_ms / 1e3) / 1e12 / int_peak, 4)}
+    cpu = None if (args.no_cpu or args.all_promotions) else cpu_baseline_sample(boards, stm, depth)
     line = {
         "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(sum(step_ms) / len(step_ms), 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic (seeded random playouts)",
         "config": {**perft_config(n), "leaves_per_step_per_gpu": int(ref_counts.sum()),
+                   "promotions": ("queen, rook, bishop, knight (not the reference's rule)" if args.all_promotions
+                                  else "queen only (the reference's rule)"),
                    "l2": "flushed between timed steps (256 MB write)", "parallelism": f"replicas x{world}",
                    "perft_config": z.perft_config()},
         "e2e": {"value": round(e2e_value, 1), "unit": UNIT, "h2d_bytes_per_step": n * 58,
@@ -668,6 +681,7 @@ def run_smp(args):
     world, rank, local = dist_env()
     torch.cuda.set_device(local)
     z.init(local, args.tt1_mb, args.tt2_mb)
+    z.engine_set_helper_depth(args.deep_every)
     depth = args.depth or 12
     wlist = [args.workers] if args.workers else [int(x) for x in args.smp_workers.split(",")]
     b = z.STARTPOS
@@ -712,6 +726,8 @@ def run_smp(args):
             "config": {"workload": f"startpos iterative deepening 1..{depth}, {args.tt1_mb} MB TT1 + {args.tt2_mb} MB "
                                    "TT2, fresh tables",
                        "workers": best["workers"], "statistic": f"median of {len(reps)} runs",
+                       "helper_depth": (f"every {args.deep_every}th helper one ply deeper" if args.deep_every
+                                        else "all workers at the iteration depth (the reference's)"),
                        "runs_s": [r["seconds"] for r in reps]},
             "nodes_per_s": best["nps"],
             "e2e": {"value": best["seconds"], "unit": "s", "h2d_bytes_per_step": 58 * best["launches"],
@@ -851,6 +867,8 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--n", type=int, default=0, help="positions per GPU (default: the workload's 4096)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the timed CPU baseline (profiling runs)")
+    ap.add_argument("--all-promotions", action="store_true",
+                    help="perft promotes to all four pieces (not the reference's rule: no CPU baseline or roofline)")
     ap.add_argument("--no-search", action="store_true",
                     help="default workload: leave out the batched-search and learned-ordering blocks")
     ap.add_argument("--ab-n", type=int, default=0,
@@ -868,6 +886,8 @@ def main():
                     help="search_batch launch form with --workers: 0 auto, 1 dense, 2 sparse, 3 warp-cooperative")
     ap.add_argument("--tt1-mb", type=int, default=2048, help="smp: transposition table size")
     ap.add_argument("--smp-workers", default="64,128,192,256,384,512,1024", help="smp: worker counts of the sweep")
+    ap.add_argument("--deep-every", type=int, default=0,
+                    help="smp: every k-th lazy-SMP helper searches one ply deeper (0 = off, the reference's search)")
     ap.add_argument("--tt2-mb", type=int, default=0,
                     help="smp: ABDADA table size (0 = no TT2: helpers randomise their move order instead)")
     args = ap.parse_args()

@@ -69,6 +69,12 @@ clrun_bool clrun_write_config(const char *path, uint64_t workers, uint64_t nps, 
  * reference's search with its heuristics (the default). */
 void cl_set_pure_search(int on);
 
+/* No counterpart in the reference: with on != 0, cl_run_perft lets a pawn
+ * promote to a queen, rook, bishop or knight (four moves); the default is
+ * the reference's queen-only rule (zetaperft.cl:1380-1384).  Kept across
+ * cl_release_device / cl_init_device. */
+void cl_set_all_promotions(int on);
+
 /* The reference's globals that the calls above read and write, with the
  * reference's types (src/zeta.h:35-139; defined by the host, src/zeta.c). */
 extern uint64_t *GLOBAL_BOARD;       /* Bitboard[7], the position to search */

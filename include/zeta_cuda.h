@@ -50,7 +50,8 @@ const char *zeta_last_error(void);
 int zeta_device_info(int *sm_count, int *cc_major, int *cc_minor, uint64_t *hbm_bytes);
 
 /* ------------------------------------------------------------------ */
-/* Perft (leaf count of the legal tree, queen-only promotions).
+/* Perft (leaf count of the legal tree; promotions to a queen only, as the
+ * reference generates them, unless zeta_perft_set_promotions(1)).
  * Replaces cl_run_perft (src/clrun.c:979-1147) + the COUNTERS read-back
  * and sum of src/search.c:225-271.  Host buffers. */
 int zeta_perft(const uint64_t board[7], int stm, int depth, uint64_t *leaves);
@@ -102,6 +103,16 @@ typedef struct {
 } zeta_perft_config;
 int zeta_perft_configure(const zeta_perft_config *cfg);
 int zeta_perft_get_config(zeta_perft_config *cfg);
+
+/* Promotion rule of every perft entry (zeta_perft, zeta_perft_batch,
+ * zeta_perft_batch_device, zeta_perft_batch_noalloc): 0 (the default, and
+ * the reference's rule, zetaperft.cl:1380-1384) a pawn reaching the last
+ * rank becomes a queen; 1 it may become a queen, rook, bishop or knight
+ * (four moves).  Lasts until changed or zeta_release.  No counterpart in
+ * the reference.  Returns ZETA_ERR_ARG for other values;
+ * zeta_perft_get_promotions gives the current rule. */
+int zeta_perft_set_promotions(int all);
+int zeta_perft_get_promotions(void);
 
 /* Statistics of the last perft launch: subtree tasks, tasks taken from
  * another block's range, interior nodes generated, leaf-parent nodes
@@ -174,6 +185,15 @@ int zeta_search_set_helpers(int max_workers_per_position);
  * and node counts do.  No counterpart in the reference (one OpenCL work
  * group per worker, zeta.cl:852). */
 int zeta_search_set_launch_form(int form);
+/* Full engine with more than one worker and no TT2 (lazy SMP, whose
+ * helpers randomise their move order, zeta.cl:1980-2001): with every = k
+ * >= 2, helpers k-1, 2k-1, ... search one ply deeper than the launch's
+ * depth.  They never end the search -- the result is that of a worker at
+ * the launch's depth -- and their table entries serve the next
+ * iterative-deepening step.  0 (the default) keeps every worker at the
+ * launch's depth, as the reference does.  Worker 0, and so a one-worker
+ * search, is never affected.  No counterpart in the reference. */
+int zeta_engine_set_helper_depth(int every);
 /* zero the transposition tables (as a new game does, src/xboard.c:159-199) */
 int zeta_tt_clear(void);
 /* device time of the last search kernel, ms */
@@ -274,7 +294,9 @@ int zeta_int_peak(double *tops);
  * generator: 0 the perft generator, 1 the search kernels' (one thread per
  * position), 2 the warp-cooperative search's (one warp per position; the
  * same list as 1, in the same order).  All give the same set; the order
- * within a list differs between 0 and the others.  Host buffers. */
+ * within a list differs between 0 and the others.  Bit 3 (perft generator
+ * only) adds the rook, bishop and knight promotions after each queen
+ * promotion.  Host buffers. */
 int zeta_genmoves_batch(const uint64_t *boards, const uint8_t *stm, int n, int flags, uint32_t *moves,
                         int32_t *counts);
 /* Static evaluation on the device (test and tooling entry): the reference

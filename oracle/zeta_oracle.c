@@ -342,7 +342,21 @@ static Move decode_move(const u64 *b, int stm, int lid, int sqto) {
   return MKMOVE(lid, sqto, sqcpt, pfrom, pto, pcpt);
 }
 
-int zo_genmoves(const zo_u64 board[7], int stm, int qs, zo_move *moves) {
+/* Append move m and, when all_promotions is set and m is a promotion,
+ * the same move promoting to a rook, a bishop and a knight (the
+ * reference stops at the queen, zetaperft.cl:1380-1384). */
+static int push_move(Move *moves, int n, Move m, int all_promotions) {
+  moves[n++] = m;
+  if (all_promotions && PTYPE(PFROM(m)) == PAWN && PTYPE(PTO(m)) == QUEEN) {
+    const int side = PFROM(m) & 1;
+    const int under[3] = {ROOK, BISHOP, KNIGHT};
+    for (int i = 0; i < 3; i++)
+      moves[n++] = MKMOVE(SQFROM(m), SQTO(m), SQCPT(m), PFROM(m), (under[i] << 1) | side, PCPT(m));
+  }
+  return n;
+}
+
+int zo_genmoves_ex(const zo_u64 board[7], int stm, int qs, int all_promotions, zo_move *moves) {
   u64 lanes[64];
   int kic;
   gen_lanes(board, stm, qs, board[PMVD], lanes, &kic);
@@ -351,10 +365,14 @@ int zo_genmoves(const zo_u64 board[7], int stm, int qs, zo_move *moves) {
     u64 t = lanes[lid];
     while (t) {
       int to = lsb(t); t &= t - 1;
-      moves[n++] = decode_move(board, stm, lid, to);
+      n = push_move(moves, n, decode_move(board, stm, lid, to), all_promotions);
     }
   }
   return n;
+}
+
+int zo_genmoves(const zo_u64 board[7], int stm, int qs, zo_move *moves) {
+  return zo_genmoves_ex(board, stm, qs, 0, moves);
 }
 
 int zo_movecount(const zo_u64 board[7], int stm, int *in_check) {
@@ -443,7 +461,7 @@ void zo_play(zo_u64 board[7], int stm, zo_move m, int perft_flags) {
 /* ------------------------------------------------------------------ */
 /* perft_gpu leaf count: a leaf is a node reached after `depth` moves
  * (sd > search_depth, zetaperft.cl:1316-1324). */
-static u64 perft_rec(u64 *b, int stm, int depth) {
+static u64 perft_rec(u64 *b, int stm, int depth, int all_promotions) {
   if (depth == 0) return 1;
   u64 lanes[64];
   int kic;
@@ -453,21 +471,26 @@ static u64 perft_rec(u64 *b, int stm, int depth) {
     u64 t = lanes[lid];
     while (t) {
       int to = lsb(t); t &= t - 1;
-      Move m = decode_move(b, stm, lid, to);
-      u64 c[7];
-      memcpy(c, b, sizeof c);
-      zo_play(c, stm, m, 1);
-      total += perft_rec(c, !stm, depth - 1);
+      Move ms[4];
+      const int k = push_move(ms, 0, decode_move(b, stm, lid, to), all_promotions);
+      for (int i = 0; i < k; i++) {
+        u64 c[7];
+        memcpy(c, b, sizeof c);
+        zo_play(c, stm, ms[i], 1);
+        total += perft_rec(c, !stm, depth - 1, all_promotions);
+      }
     }
   }
   return total;
 }
 
-zo_u64 zo_perft(const zo_u64 board[7], int stm, int depth) {
+zo_u64 zo_perft_ex(const zo_u64 board[7], int stm, int depth, int all_promotions) {
   u64 b[7];
   memcpy(b, board, sizeof b);
-  return perft_rec(b, stm, depth);
+  return perft_rec(b, stm, depth, all_promotions);
 }
+
+zo_u64 zo_perft(const zo_u64 board[7], int stm, int depth) { return zo_perft_ex(board, stm, depth, 0); }
 
 /* ------------------------------------------------------------------ */
 /* Evaluation x64 + bishop pair, zeta.cl:1479-1531 (white's view). */

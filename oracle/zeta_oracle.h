@@ -48,6 +48,12 @@ zo_u64 zo_computehash(const zo_u64 board[7], int stm);
  * Order: lane (from-square) ascending, then to-square ascending. */
 int zo_genmoves(const zo_u64 board[7], int stm, int qs, zo_move *moves);
 
+/* The same with all_promotions != 0: each queen promotion is followed by
+ * the same move promoting to a rook, a bishop and a knight.  The reference
+ * generates queen promotions only; this rule has no reference output to
+ * pin, so the tests pin it against an independent mailbox generator. */
+int zo_genmoves_ex(const zo_u64 board[7], int stm, int qs, int all_promotions, zo_move *moves);
+
 /* Number of legal moves and the reference's in-check flag. */
 int zo_movecount(const zo_u64 board[7], int stm, int *in_check);
 
@@ -59,6 +65,8 @@ void zo_play(zo_u64 board[7], int stm, zo_move move, int perft_flags);
 
 /* Leaf count of the legal tree (queen-only promotions), zetaperft.cl:801-1477. */
 zo_u64 zo_perft(const zo_u64 board[7], int stm, int depth);
+/* The same with all four promotions when all_promotions != 0. */
+zo_u64 zo_perft_ex(const zo_u64 board[7], int stm, int depth, int all_promotions);
 
 /* Static evaluation, white's view, zeta.cl:1479-1544 (x64 lanes + bishop pair). */
 int zo_eval_white(const zo_u64 board[7]);

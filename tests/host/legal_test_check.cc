@@ -9,6 +9,9 @@
  *     flag;
  *   - the search kernels' generator (gen_engine) gives the perft
  *     generator's (gen_legal) move set, all moves and captures only;
+ *   - with all four promotions, the perft generator (gen_legal<true>)
+ *     gives the oracle's zo_genmoves_ex set and its bulk count
+ *     (count_legal_ex<true>) that set's size;
  *   - the warp generator's plan and per-move decode (warpgen.cuh), in
  *     both their unrolled and rolled forms, give gen_engine's list move for
  *     move, in the same order, and the same in-check flag;
@@ -103,6 +106,21 @@ static void walk(const Pos &p, int stm, int depth) {
     std::sort(b, b + nb);
     if (na != nb || !std::equal(a, a + na, b)) {
       if (g_bad < 5) printf("generators differ (qs %d): %d vs %d moves\n", qs, na, nb);
+      g_bad++;
+    }
+  }
+  /* all four promotions: the perft generator and its bulk count against
+   * the oracle's all-promotions mode */
+  for (int qs = 0; qs < 2; qs++) {
+    Move a[256];
+    zo_move o[256];
+    const int na = gen_legal<true>(p, stm, qs != 0, a);
+    const int no = zo_genmoves_ex(b7, stm, qs, 1, o);
+    bool ck;
+    std::sort(a, a + na);
+    std::sort(o, o + no);
+    if (na != no || !std::equal(a, a + na, o) || (!qs && count_legal_ex<true>(p, stm, ck) != na)) {
+      if (g_bad < 5) printf("all-promotions generator differs (qs %d): %d vs %d moves\n", qs, na, no);
       g_bad++;
     }
   }

@@ -27,6 +27,7 @@ def oracle() -> ctypes.CDLL:
             subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle")], check=True)
         o = ctypes.CDLL(ORACLE_SO)
         o.zo_perft.restype = ctypes.c_uint64
+        o.zo_perft_ex.restype = ctypes.c_uint64
         o.zo_computehash.restype = ctypes.c_uint64
         o.zo_splitmix64.restype = ctypes.c_uint64
         o.zo_can2move.restype = ctypes.c_uint32
@@ -68,7 +69,9 @@ def _b7(board) -> ctypes.Array:
     return _B7(*[int(x) for x in np.asarray(board, dtype=np.uint64).reshape(7)])
 
 
-def perft(board, stm: int, depth: int) -> int:
+def perft(board, stm: int, depth: int, all_promotions: bool = False) -> int:
+    if all_promotions:
+        return oracle().zo_perft_ex(_b7(board), int(stm), int(depth), 1)
     return oracle().zo_perft(_b7(board), int(stm), int(depth))
 
 
@@ -131,9 +134,9 @@ class RefSearch:
             self.h = None
 
 
-def genmoves(board, stm: int, qs: bool = False) -> list[int]:
+def genmoves(board, stm: int, qs: bool = False, all_promotions: bool = False) -> list[int]:
     buf = (ctypes.c_uint32 * 256)()
-    n = oracle().zo_genmoves(_b7(board), int(stm), int(qs), buf)
+    n = oracle().zo_genmoves_ex(_b7(board), int(stm), int(qs), int(all_promotions), buf)
     return list(buf[:n])
 
 

@@ -200,3 +200,45 @@ def test_engine_launch_forms_match_reference(zeta_device, form):
         pv_r, c_r = ref.run(boards[i], int(stm[i]), 5)
         assert list(pvs[i]) == list(pv_r), (form, i)
         assert sc[i] == np.int32(pv_r[0]) and mv[i] == pv_r[1] and nodes[i] == c_r[0, 1]
+
+
+def test_engine_deeper_helpers(zeta_device):
+    """Lazy SMP (no TT2) with every second helper one ply deeper
+    (zeta_engine_set_helper_depth): worker 0 -- and so a one-worker search
+    -- still visits exactly the reference's tree, and a 16-worker
+    iterative deepening ends every depth with a legal PV from a worker at
+    that depth."""
+    _need_reference()
+    z = zeta_device
+    z.release()
+    z.init(0, 64, 0)
+    try:
+        z.engine_set_helper_depth(2)
+        b, stm = ol.setboard("rnbqkbnr/pppppppp/8/8/8/8/PPPPPPPP/RNBQKBNR w KQkq - 0 1")
+        ref = ol.RefSearch(E1, 0)
+        z.tt_clear()
+        for d in range(1, 6):
+            pv_r, c_r = ref.run(b, stm, d)
+            pv_g, c_g = z.engine_search(b, stm, d, 1)
+            assert list(pv_g) == list(pv_r) and list(c_g[0, SLOTS]) == list(c_r[0, SLOTS]), d
+        w = z.WORKLOADS["engine"]
+        boards, stms, _ = ol.make_positions(w["seed"] + 3, 2, min_plies=w["min_plies"], max_plies=w["max_plies"],
+                                            min_pieces=w["min_pieces"], min_depth=0, max_depth=0)
+        for i in range(2):
+            z.tt_clear()
+            for d in range(1, 8):
+                pv, cnt = z.engine_search(boards[i], int(stms[i]), d, 16)
+                assert pv[1] != 0 and cnt[:, 1].sum() > 0, (i, d)
+                cur, s = boards[i].copy(), int(stms[i])
+                for m in pv[1:1 + d]:
+                    if m == 0:
+                        break
+                    assert int(m) in ol.genmoves(cur, s), (i, d, ol.move2can(int(m)))
+                    cur = ol.play(cur, s, int(m))
+                    s ^= 1
+        with pytest.raises(z.ZetaError):
+            z.engine_set_helper_depth(1)
+    finally:
+        z.engine_set_helper_depth(0)
+        z.release()
+        z.init(0, 64, 16)

@@ -79,6 +79,8 @@ SIGNATURES = {
                                                 ctypes.c_void_p, ctypes.c_void_p]),
     "zeta_perft_configure": (ctypes.c_int, [ctypes.POINTER(PerftConfig)]),
     "zeta_perft_get_config": (ctypes.c_int, [ctypes.POINTER(PerftConfig)]),
+    "zeta_perft_set_promotions": (ctypes.c_int, [ctypes.c_int]),
+    "zeta_perft_get_promotions": (ctypes.c_int, []),
     "zeta_perft_last_stats": (ctypes.c_int, [ctypes.POINTER(PerftStats)]),
     "zeta_make_positions": (ctypes.c_int, [ctypes.c_uint64, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                            ctypes.c_int, ctypes.c_int, _u64p, _u8p, _u8p]),
@@ -116,6 +118,7 @@ SIGNATURES = {
     "zeta_tt_clear": (ctypes.c_int, []),
     "zeta_search_set_helpers": (ctypes.c_int, [ctypes.c_int]),
     "zeta_search_set_launch_form": (ctypes.c_int, [ctypes.c_int]),
+    "zeta_engine_set_helper_depth": (ctypes.c_int, [ctypes.c_int]),
     "zeta_search_last_ms": (ctypes.c_int, [ctypes.POINTER(ctypes.c_float)]),
     "zeta_genmoves_batch": (ctypes.c_int, [_u64p, _u8p, ctypes.c_int, ctypes.c_int, _u32p, _i32p]),
     "zeta_eval_batch": (ctypes.c_int, [_u64p, ctypes.c_int, _i32p]),
@@ -203,6 +206,16 @@ def perft_config() -> dict:
     return {f: getattr(cfg, f) for f, _ in PerftConfig._fields_}
 
 
+def perft_set_promotions(all_pieces: bool) -> None:
+    """Promotion rule of every perft entry: False (default) queen only, as
+    the reference; True queen, rook, bishop or knight."""
+    _check(load_library().zeta_perft_set_promotions(1 if all_pieces else 0))
+
+
+def perft_get_promotions() -> bool:
+    return load_library().zeta_perft_get_promotions() == 1
+
+
 def perft_stats() -> dict:
     st = PerftStats()
     _check(load_library().zeta_perft_last_stats(ctypes.byref(st)))
@@ -241,6 +254,11 @@ def search_batch_device(d_boards: int, d_stm: int, n: int, depth: int, workers: 
 
 def search_set_helpers(max_workers_per_position: int) -> None:
     _check(load_library().zeta_search_set_helpers(max_workers_per_position))
+
+
+def engine_set_helper_depth(every: int) -> None:
+    """Full engine, lazy SMP: every `every`-th helper one ply deeper (0 = off)."""
+    _check(load_library().zeta_engine_set_helper_depth(int(every)))
 
 
 def search_set_launch_form(form: int) -> None:
@@ -409,14 +427,18 @@ def int_peak_tops() -> float:
     return t.value
 
 
-def genmoves_batch(boards: np.ndarray, stm: np.ndarray, qs: bool = False, generator: int = 0):
-    """Legal moves on the device; generator 0 the perft generator, 1 the search kernels'."""
+def genmoves_batch(boards: np.ndarray, stm: np.ndarray, qs: bool = False, generator: int = 0,
+                   all_promotions: bool = False):
+    """Legal moves on the device; generator 0 the perft generator, 1 the
+    search kernels', 2 the warp-cooperative search's; all_promotions (perft
+    generator only) adds the rook, bishop and knight promotions."""
     b = np.ascontiguousarray(boards, dtype=np.uint64).reshape(-1, 7)
     s = np.ascontiguousarray(stm, dtype=np.uint8)
     n = b.shape[0]
     moves = np.zeros((n, 256), dtype=np.uint32)
     counts = np.zeros(n, dtype=np.int32)
-    _check(load_library().zeta_genmoves_batch(_ptr(b, _u64p), _ptr(s, _u8p), n, int(qs) | (generator << 1), _ptr(moves, _u32p),
+    flags = int(qs) | (generator << 1) | (8 if all_promotions else 0)
+    _check(load_library().zeta_genmoves_batch(_ptr(b, _u64p), _ptr(s, _u8p), n, flags, _ptr(moves, _u32p),
                                               _ptr(counts, _i32p)))
     return [moves[i, : counts[i]].copy() for i in range(n)]
 

@@ -175,6 +175,14 @@ int zeta_perft_get_config(zeta_perft_config *cfg) {
   return ZETA_OK;
 }
 
+int zeta_perft_set_promotions(int all) {
+  if (all != 0 && all != 1) return set_error(ZETA_ERR_ARG, "promotions: 0 (queen only) or 1 (all four pieces)");
+  g_ctx.perft_allp = all;
+  return ZETA_OK;
+}
+
+int zeta_perft_get_promotions(void) { return g_ctx.perft_allp; }
+
 int zeta_perft_last_stats(zeta_perft_stats *st) {
   if (!st) return set_error(ZETA_ERR_ARG, "null stats");
   *st = g_ctx.pstats;
@@ -354,6 +362,12 @@ int zeta_search_set_learned_order(int top, int quiet_only) {
 int zeta_search_set_helpers(int max_workers_per_position) {
   if (max_workers_per_position < 0) return set_error(ZETA_ERR_ARG, "negative helper cap");
   g_ctx.s_helpers_cap = max_workers_per_position;
+  return ZETA_OK;
+}
+
+int zeta_engine_set_helper_depth(int every) {
+  if (every < 0 || every == 1) return set_error(ZETA_ERR_ARG, "helper depth: 0 (off) or every k-th helper, k >= 2");
+  g_ctx.e_deep_every = every;
   return ZETA_OK;
 }
 

@@ -56,6 +56,8 @@ enum { PNONE = 0, PAWN = 1, KNIGHT = 2, KING = 3, BISHOP = 4, ROOK = 5, QUEEN = 
 #define ZETA_RANK4 0x00000000FF000000ULL
 #define ZETA_RANK5 0x000000FF00000000ULL
 #define ZETA_RANK6 0x0000FF0000000000ULL
+#define ZETA_RANK1 0x00000000000000FFULL
+#define ZETA_RANK8 0xFF00000000000000ULL
 #define ZETA_NULLMOVE 0x41u
 
 /* A position without hash and clock: what move generation needs. */
@@ -314,7 +316,10 @@ ZHD u64 slider_targets(const Sets &s, const Guard &g, u64 tgt) {
 
 /* ---------------- bulk count ----------------
  * Number of legal moves: the leaf count of a node one ply above the
- * leaves, without expanding it. */
+ * leaves, without expanding it.  ALLP: a pawn reaching the last rank
+ * makes four moves (queen, rook, bishop, knight) instead of the
+ * reference's one queen promotion. */
+template <bool ALLP = false>
 ZHD int count_legal_ex(const Pos &p, int stm, bool &in_check) {
   Sets s = make_sets(p, stm);
   Guard g = make_guard(s, stm);
@@ -346,6 +351,7 @@ ZHD int count_legal_ex(const Pos &p, int stm, bool &in_check) {
   }
   n += popc(s1 & g.cmask) + popc(s2 & g.cmask) + popc(c1 & s.them & g.cmask) +
        popc(c2 & s.them & g.cmask);
+  if (ALLP) n += 3 * popc((s1 | ((c1 | c2) & s.them)) & g.cmask & (stm ? ZETA_RANK1 : ZETA_RANK8));
   u64 N = s.knights & s.us & free_;
   n += popc(((N << 17) & ZETA_NOTA) & tgt) + popc(((N << 15) & ZETA_NOTH) & tgt) +
        popc(((N << 10) & ZETA_NOTAB) & tgt) + popc(((N << 6) & ZETA_NOTGH) & tgt) +
@@ -359,9 +365,10 @@ ZHD int count_legal_ex(const Pos &p, int stm, bool &in_check) {
   return n;
 }
 
+template <bool ALLP = false>
 ZHD int count_legal(const Pos &p, int stm) {
   bool in_check;
-  return count_legal_ex(p, stm, in_check);
+  return count_legal_ex<ALLP>(p, stm, in_check);
 }
 
 /* A quick sufficient test for "the side to move has a legal move": out of
@@ -491,8 +498,32 @@ ZHD int emit_shift(const Pos &p, int stm, u64 t, int delta, Move *list, int n) {
   return n;
 }
 
+/* Single pushes and pawn captures.  encode() makes a pawn reaching the
+ * last rank a queen, as the reference does; with ALLP the rook, bishop
+ * and knight promotions follow it (same squares, pieces, capture). */
+template <bool ALLP>
+ZHD int emit_pawn(const Pos &p, int stm, u64 t, int delta, Move *list, int n) {
+  if (ALLP) {
+    const u64 last = stm ? ZETA_RANK1 : ZETA_RANK8;
+    u64 pr = t & last;
+    t &= ~last;
+    while (pr) {
+      const int to = ctz(pr);
+      pr &= pr - 1;
+      const Move q = encode(p, stm, to - delta, to);
+      const Move rest = q & ~(15u << 22);
+      list[n++] = q;
+      list[n++] = rest | ((Move)((ROOK << 1) | stm) << 22);
+      list[n++] = rest | ((Move)((BISHOP << 1) | stm) << 22);
+      list[n++] = rest | ((Move)((KNIGHT << 1) | stm) << 22);
+    }
+  }
+  return emit_shift(p, stm, t, delta, list, n);
+}
+
 /* the same with the side's piece sets and the enemy attack map already
  * computed (callers that also need the in-check test) */
+template <bool ALLP = false>
 ZHD int gen_legal_sd(const Pos &p, const Sets &s, u64 danger, int stm, bool qs, Move *list) {
   Guard g = make_guard(s, stm);
   u64 capmask = qs ? s.them : ~0ULL;
@@ -516,20 +547,20 @@ ZHD int gen_legal_sd(const Pos &p, const Sets &s, u64 danger, int stm, bool qs, 
     u64 s1 = (pp >> 8) & empty;
     u64 s2 = ((s1 & ZETA_RANK6) >> 8) & empty;
     if (!qs) {
-      n = emit_shift(p, stm, s1 & g.cmask, -8, list, n);
+      n = emit_pawn<ALLP>(p, stm, s1 & g.cmask, -8, list, n);
       n = emit_shift(p, stm, s2 & g.cmask, -16, list, n);
     }
-    n = emit_shift(p, stm, ((pa >> 7) & ZETA_NOTA) & s.them & g.cmask, -7, list, n);
-    n = emit_shift(p, stm, ((pd >> 9) & ZETA_NOTH) & s.them & g.cmask, -9, list, n);
+    n = emit_pawn<ALLP>(p, stm, ((pa >> 7) & ZETA_NOTA) & s.them & g.cmask, -7, list, n);
+    n = emit_pawn<ALLP>(p, stm, ((pd >> 9) & ZETA_NOTH) & s.them & g.cmask, -9, list, n);
   } else {
     u64 s1 = (pp << 8) & empty;
     u64 s2 = ((s1 & ZETA_RANK3) << 8) & empty;
     if (!qs) {
-      n = emit_shift(p, stm, s1 & g.cmask, 8, list, n);
+      n = emit_pawn<ALLP>(p, stm, s1 & g.cmask, 8, list, n);
       n = emit_shift(p, stm, s2 & g.cmask, 16, list, n);
     }
-    n = emit_shift(p, stm, ((pd << 9) & ZETA_NOTA) & s.them & g.cmask, 9, list, n);
-    n = emit_shift(p, stm, ((pa << 7) & ZETA_NOTH) & s.them & g.cmask, 7, list, n);
+    n = emit_pawn<ALLP>(p, stm, ((pd << 9) & ZETA_NOTA) & s.them & g.cmask, 9, list, n);
+    n = emit_pawn<ALLP>(p, stm, ((pa << 7) & ZETA_NOTH) & s.them & g.cmask, 7, list, n);
   }
   u64 N = s.knights & s.us & free_;
   n = emit_shift(p, stm, ((N << 17) & ZETA_NOTA) & tgt, 17, list, n);
@@ -565,9 +596,10 @@ ZHD int gen_legal_sd(const Pos &p, const Sets &s, u64 danger, int stm, bool qs, 
   return n;
 }
 
+template <bool ALLP = false>
 ZHD int gen_legal(const Pos &p, int stm, bool qs, Move *list) {
   const Sets s = make_sets(p, stm);
-  return gen_legal_sd(p, s, enemy_attacks(s, stm), stm, qs, list);
+  return gen_legal_sd<ALLP>(p, s, enemy_attacks(s, stm), stm, qs, list);
 }
 
 }  // namespace zeta

@@ -83,6 +83,7 @@ struct Context {
 
   /* the autotuner's choice on GB300 (zeta_gb300/perft_tuned.json) */
   zeta_perft_config pcfg{256, 3, 0, 4, 1};
+  int perft_allp = 0; /* 1: perft promotes to all four pieces; 0: queen only, the reference's rule */
   zeta_perft_stats pstats{};
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   cudaEvent_t ev_join[2] = {nullptr, nullptr}; /* ordering with a caller's stream */
@@ -93,6 +94,7 @@ struct Context {
   int g_n = -1;
   cudaStream_t g_stream = nullptr;
   zeta_perft_config g_cfg{};
+  int g_allp = 0;
 
   /* transposition tables (search) */
   void *mlp = nullptr; /* move-ordering network state (mlp.cu) */
@@ -109,6 +111,7 @@ struct Context {
   uint32_t *s_status = nullptr;
   int s_helpers_cap = 0;      /* max workers per position once helpers join; 0 = no helpers */
   int s_launch_form = 0;      /* search kernels: 0 auto, 1 dense, 2 sparse, 3 warp (pure search) */
+  int e_deep_every = 0;       /* full engine, lazy SMP: every k-th helper one ply deeper (0 = off) */
   int s_learned_top = 12;     /* network moves used by the learned ordering */
   int s_learned_quiet = 1;    /* 1: they order the quiet moves only */
   void *s_ocache = nullptr;   /* learned ordering: OrderEntry cache */

@@ -187,6 +187,7 @@ int engine_launch(int n, int w, int depth, uint64_t max_nodes, bool with_hist, b
   a.finito = e.finito;
   a.pv = e.pv;
   a.status = e.status;
+  a.deep_every = c.e_deep_every;
   if (learned) {
     a.ocache = (OrderEntry *)c.s_ocache;
     a.ocache_mask = c.s_ocache_entries - 1;

@@ -136,6 +136,10 @@ struct EngineArgs {
   uint32_t *noreq;
   uint32_t oreq_cap;
   int learned_top;
+  /* lazy SMP (no TT2) helper depths, no reference counterpart: with k >= 2,
+   * helpers w = k-1, 2k-1, ... search one ply deeper than the iteration;
+   * 0 = every worker at the iteration depth (the reference's search) */
+  int deep_every;
 };
 
 /* the move-ordering score of the reference's picker (zeta.cl:2087-2124) */
@@ -342,7 +346,10 @@ __host__ __device__ void engine_worker(const EngineArgs &a, long long t, const E
   TT2E *tt2 = a.tt2_slice > 1 ? a.tt2 + (u64)p * a.tt2_slice : nullptr;
   const u64 mask1 = a.tt1_slice - 1, mask2 = a.tt2_slice - 1;
   const int gid1 = w + 1;
-  const int D = a.depth;
+  /* a deeper helper never ends the search (the result is a worker's at the
+   * iteration depth); its table entries serve the next iteration */
+  const bool deeper = !tt2 && a.deep_every >= 2 && w > 0 && w % a.deep_every == a.deep_every - 1;
+  const int D = a.depth + (deeper ? 1 : 0);
   const int ply_init = a.ply_init ? a.ply_init[p] : 0;
   const int ttage = ply_init & 0x3F;
   const uint64_t *B = a.boards + (long long)p * 7;
@@ -562,7 +569,7 @@ __host__ __device__ void engine_worker(const EngineArgs &a, long long t, const E
       ply--;
       stm ^= 1;
       if (sd < 1) {
-        e_casu(a.finito + p, 0u, (uint32_t)gid1); /* early bird */
+        if (!deeper) e_casu(a.finito + p, 0u, (uint32_t)gid1); /* early bird */
         break;
       }
       EFrame *g = F + sd;

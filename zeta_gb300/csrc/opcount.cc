@@ -232,7 +232,7 @@ int main(int argc, char **argv) {
           "counted)\"\n}\n",
           a.count_nodes, (double)a.count_ops / a.count_nodes, a.gen_nodes, (double)a.gen_ops / a.gen_nodes,
           b.count_nodes, (double)b.count_ops / b.count_nodes, b.gen_nodes, (double)b.gen_ops / b.gen_nodes,
-          (double)b.count_ops / b.count_nodes, (double)b.gen_ops / b.gen_nodes, st.leaves, s_leaf, st.interior, s_int,
+          (double)a.count_ops / a.count_nodes, (double)a.gen_ops / a.gen_nodes, st.leaves, s_leaf, st.interior, s_int,
           s_node, e_node);
   fclose(f);
   printf("search node: %.1f ops (horizon %.1f, interior %.1f); engine node: %.1f ops\n", s_node, s_leaf, s_int, e_node);

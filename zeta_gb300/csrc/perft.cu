@@ -24,6 +24,11 @@
  * instead of expanding them.  The counting phase, which is nearly all of
  * the work, runs with no divergence between threads.
  *
+ * Promotions follow the reference (queen only) unless the caller asks for
+ * all four pieces (zeta_perft_set_promotions): every kernel that generates
+ * or counts moves is compiled in both forms (template flag ALLP), so the
+ * reference's form pays nothing for the other.
+ *
  * The sequence is captured in a CUDA graph and replayed while the batch
  * shape stays the same.  Leaf counts are u64 and summed with atomics, so
  * the result does not depend on scheduling.
@@ -76,6 +81,7 @@ __global__ void k_roots(const uint64_t *__restrict__ boards, const uint8_t *__re
 }
 
 /* One split level: see the file comment. */
+template <bool ALLP>
 __global__ void __launch_bounds__(128) k_split(int level, const Task *__restrict__ in, Task *__restrict__ out,
                                                Task *__restrict__ fin, uint32_t cap_lvl, uint32_t cap_fin,
                                                uint32_t min_tasks, int rmax, PerftCounters *pc) {
@@ -103,7 +109,7 @@ __global__ void __launch_bounds__(128) k_split(int level, const Task *__restrict
       else atomicOr(&pc->status, ST_CAPACITY);
       continue;
     }
-    int nm = gen_legal(t.pos, t.stm, false, list);
+    int nm = gen_legal<ALLP>(t.pos, t.stm, false, list);
     interior++;
     if (nm == 0) continue;
     uint32_t k = atomicAdd(&pc->level_n[level + 1], (uint32_t)nm);
@@ -187,19 +193,21 @@ __device__ __forceinline__ unsigned long long block_sum(unsigned long long v, un
 /* One copy of each generator in the kernel's code: the kernels call them
  * from several places, and inlining every call overflows the
  * instruction cache. */
-__device__ __noinline__ int count_node(Pos p, int stm) { return count_legal(p, stm); }
-__device__ __noinline__ int expand_node(Pos p, int stm, Move *list) { return gen_legal(p, stm, false, list); }
+template <bool ALLP>
+__device__ __noinline__ int count_node(Pos p, int stm) { return count_legal<ALLP>(p, stm); }
+template <bool ALLP>
+__device__ __noinline__ int expand_node(Pos p, int stm, Move *list) { return gen_legal<ALLP>(p, stm, false, list); }
 
 /* Expand src[0..nsrc) (nsrc <= TPB, one node per thread) into dst,
  * children of a node contiguous; returns the number written.  Block-wide:
  * every thread must call it. */
-template <int TPB>
+template <int TPB, bool ALLP>
 __device__ __forceinline__ int expand_round(const Pos *src, int nsrc, int stm, Pos *dst, int dst_cap, int *s_warp,
                                             Move *list, unsigned long long &interior, uint32_t *status) {
   const int tid = threadIdx.x;
   int k = 0;
   if (tid < nsrc) {
-    k = expand_node(src[tid], stm, list);
+    k = expand_node<ALLP>(src[tid], stm, list);
     interior++;
   }
   int off;
@@ -218,11 +226,11 @@ __device__ __forceinline__ int expand_round(const Pos *src, int nsrc, int stm, P
 }
 
 /* sum of the legal-move counts of src[0..n): the leaf count below them */
-template <int TPB>
+template <int TPB, bool ALLP>
 __device__ __forceinline__ unsigned long long count_range(const Pos *src, int n, int stm, unsigned long long &counted) {
   unsigned long long acc = 0;
   for (int j = threadIdx.x; j < n; j += TPB) {
-    acc += (unsigned)count_node(src[j], stm);
+    acc += (unsigned)count_node<ALLP>(src[j], stm);
     counted++;
   }
   return acc;
@@ -232,7 +240,7 @@ __device__ __forceinline__ unsigned long long count_range(const Pos *src, int n,
  * (218*218 covers any position) and `cap3` for the nodes one ply above the
  * leaves; each round expands at most cap3/218 parents, so it never
  * overflows. */
-template <int TPB, int MINB>
+template <int TPB, int MINB, bool ALLP>
 __global__ void __launch_bounds__(TPB, MINB) k_perft_ws(const Task *__restrict__ tasks, uint32_t *cursors,
                                                   uint64_t *__restrict__ leaves, PerftCounters *pc,
                                                   Pos *__restrict__ scratch, uint32_t cap2, uint32_t cap3,
@@ -273,12 +281,12 @@ __global__ void __launch_bounds__(TPB, MINB) k_perft_ws(const Task *__restrict__
     if (R == 0) {
       acc = tid == 0;
     } else if (R == 1) {
-      acc = count_range<TPB>(&s_root, 1, t.stm, counted);
+      acc = count_range<TPB, ALLP>(&s_root, 1, t.stm, counted);
     } else {
       /* level 1: the task root's children, in shared memory */
-      const int n1 = expand_round<TPB>(&s_root, 1, t.stm, s_l1, 256, s_warp, list, interior, &pc->status);
+      const int n1 = expand_round<TPB, ALLP>(&s_root, 1, t.stm, s_l1, 256, s_warp, list, interior, &pc->status);
       if (R == 2) {
-        acc = count_range<TPB>(s_l1, n1, t.stm ^ 1, counted);
+        acc = count_range<TPB, ALLP>(s_l1, n1, t.stm ^ 1, counted);
       } else {
         /* R == 4: level 2 in full into the block's level-2 buffer */
         const Pos *par = s_l1;
@@ -286,7 +294,7 @@ __global__ void __launch_bounds__(TPB, MINB) k_perft_ws(const Task *__restrict__
         if (R == 4) {
           int n2 = 0;
           for (int base = 0; base < n1; base += TPB)
-            n2 += expand_round<TPB>(s_l1 + base, min(TPB, n1 - base), t.stm ^ 1, b2 + n2, (int)cap2 - n2, s_warp,
+            n2 += expand_round<TPB, ALLP>(s_l1 + base, min(TPB, n1 - base), t.stm ^ 1, b2 + n2, (int)cap2 - n2, s_warp,
                                     list, interior, &pc->status);
           par = b2;
           npar = n2;
@@ -294,9 +302,9 @@ __global__ void __launch_bounds__(TPB, MINB) k_perft_ws(const Task *__restrict__
         }
         /* the nodes one ply above the leaves, a round at a time, then count */
         for (int base = 0; base < npar; base += per_round) {
-          const int total = expand_round<TPB>(par + base, min(per_round, npar - base), spar, b3, (int)cap3, s_warp,
+          const int total = expand_round<TPB, ALLP>(par + base, min(per_round, npar - base), spar, b3, (int)cap3, s_warp,
                                               list, interior, &pc->status);
-          acc += count_range<TPB>(b3, total, spar ^ 1, counted);
+          acc += count_range<TPB, ALLP>(b3, total, spar ^ 1, counted);
           __syncthreads();
         }
       }
@@ -320,10 +328,10 @@ __global__ void __launch_bounds__(TPB, MINB) k_perft_ws(const Task *__restrict__
   }
 }
 
-/* one thread per position: gen 0 the perft generator (gen_legal), 1 the
- * search engine's (gen_engine) */
+/* one thread per position: gen 0 the perft generator (gen_legal; allp:
+ * all four promotions), 1 the search engine's (gen_engine) */
 __global__ void k_genmoves(const uint64_t *__restrict__ boards, const uint8_t *__restrict__ stm, int n, int qs,
-                           int gen, uint32_t *__restrict__ moves, int32_t *__restrict__ counts) {
+                           int gen, int allp, uint32_t *__restrict__ moves, int32_t *__restrict__ counts) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   Move list[256];
@@ -332,6 +340,8 @@ __global__ void k_genmoves(const uint64_t *__restrict__ boards, const uint8_t *_
   if (gen == 1) {
     const Sets sets = make_sets(p, stm[i] & 1);
     k = gen_engine(p, sets, enemy_attacks(sets, stm[i] & 1), stm[i] & 1, qs != 0, list);
+  } else if (allp) {
+    k = gen_legal<true>(p, stm[i] & 1, qs != 0, list);
   } else {
     k = gen_legal(p, stm[i] & 1, qs != 0, list);
   }
@@ -347,20 +357,26 @@ typedef void (*WsKernel)(const Task *, uint32_t *, uint64_t *, PerftCounters *, 
  * blocks_per_sm == 0 selects the uncapped variant.  Caps of 64 registers
  * (128x8, 256x4, 512x2) are not built: 128x8 raised an illegal-address
  * fault on GB300 at task depth 3 with its bounds checks silent. */
-WsKernel ws_kernel(int tpb, int minb) {
+template <bool ALLP>
+WsKernel ws_kernel_of(int tpb, int minb) {
   switch (tpb * 100 + minb) {
-    case 6400: return k_perft_ws<64, 1>;
-    case 6408: return k_perft_ws<64, 8>;
-    case 6412: return k_perft_ws<64, 12>;
-    case 12800: return k_perft_ws<128, 1>;
-    case 12804: return k_perft_ws<128, 4>;
-    case 12806: return k_perft_ws<128, 6>;
-    case 25600: return k_perft_ws<256, 1>;
-    case 25603: return k_perft_ws<256, 3>;
-    case 51200: return k_perft_ws<512, 1>;
+    case 6400: return k_perft_ws<64, 1, ALLP>;
+    case 6408: return k_perft_ws<64, 8, ALLP>;
+    case 6412: return k_perft_ws<64, 12, ALLP>;
+    case 12800: return k_perft_ws<128, 1, ALLP>;
+    case 12804: return k_perft_ws<128, 4, ALLP>;
+    case 12806: return k_perft_ws<128, 6, ALLP>;
+    case 25600: return k_perft_ws<256, 1, ALLP>;
+    case 25603: return k_perft_ws<256, 3, ALLP>;
+    case 51200: return k_perft_ws<512, 1, ALLP>;
     default: return nullptr;
   }
 }
+WsKernel ws_kernel(int tpb, int minb, bool allp) {
+  return allp ? ws_kernel_of<true>(tpb, minb) : ws_kernel_of<false>(tpb, minb);
+}
+typedef void (*SplitKernel)(int, const Task *, Task *, Task *, uint32_t, uint32_t, uint32_t, int, PerftCounters *);
+SplitKernel split_kernel(bool allp) { return allp ? k_split<true> : k_split<false>; }
 
 }  // namespace
 
@@ -407,12 +423,12 @@ static int ensure_stack(const void *k) {
 static int ws_geometry(int &blocks, int &tpb, WsKernel &k) {
   Context &c = ctx();
   tpb = c.pcfg.threads_per_block;
-  k = ws_kernel(tpb, c.pcfg.blocks_per_sm);
+  k = ws_kernel(tpb, c.pcfg.blocks_per_sm, c.perft_allp != 0);
   if (!k)
     return set_error(ZETA_ERR_ARG, "no perft kernel variant for %d threads x %d blocks per SM", tpb,
                      c.pcfg.blocks_per_sm);
   int rc = ensure_stack((const void *)k);
-  if (!rc) rc = ensure_stack((const void *)k_split);
+  if (!rc) rc = ensure_stack((const void *)split_kernel(c.perft_allp != 0));
   if (rc) return rc;
   int bps = 0;
   ZCHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k, tpb, 0));
@@ -449,9 +465,10 @@ static int perft_enqueue(const uint64_t *d_boards, const uint8_t *d_stm, const u
   ZCHECK(cudaMemsetAsync(c.cursors, 0, blocks * sizeof(uint32_t), s));
   k_roots<<<(n + 127) / 128, 128, 0, s>>>(d_boards, d_stm, d_depth, n, c.lvl[0], d_leaves, c.pc);
   ZCHECK(cudaGetLastError());
+  const SplitKernel split = split_kernel(c.perft_allp != 0);
   for (int lv = 0; lv < kMaxLevels; lv++) {
-    k_split<<<c.sms * 4, 128, 0, s>>>(lv, c.lvl[lv & 1], c.lvl[(lv + 1) & 1], c.fin, c.cap_lvl, c.cap_fin,
-                                      min_tasks, c.pcfg.task_depth, c.pc);
+    split<<<c.sms * 4, 128, 0, s>>>(lv, c.lvl[lv & 1], c.lvl[(lv + 1) & 1], c.fin, c.cap_lvl, c.cap_fin,
+                                    min_tasks, c.pcfg.task_depth, c.pc);
     ZCHECK(cudaGetLastError());
   }
   /* external records: inside a stream capture they become event-record
@@ -504,7 +521,7 @@ int perft_run(const uint64_t *d_boards, const uint8_t *d_stm, const uint8_t *d_d
               c.g_leaves == d_leaves && c.g_n == n && c.g_stream == s &&
               c.g_cfg.threads_per_block == c.pcfg.threads_per_block &&
               c.g_cfg.blocks_per_sm == c.pcfg.blocks_per_sm && c.g_cfg.min_tasks == c.pcfg.min_tasks &&
-              c.g_cfg.task_depth == c.pcfg.task_depth;
+              c.g_cfg.task_depth == c.pcfg.task_depth && c.g_allp == c.perft_allp;
   if (c.pcfg.use_graph) {
     if (!same) {
       if (c.graph) {
@@ -527,6 +544,7 @@ int perft_run(const uint64_t *d_boards, const uint8_t *d_stm, const uint8_t *d_d
       c.g_n = n;
       c.g_stream = s;
       c.g_cfg = c.pcfg;
+      c.g_allp = c.perft_allp;
     }
     ZCHECK(cudaGraphLaunch(c.graph, s));
   } else {
@@ -559,10 +577,11 @@ int perft_run(const uint64_t *d_boards, const uint8_t *d_stm, const uint8_t *d_d
 
 int genmoves_launch(const uint64_t *d_boards, const uint8_t *d_stm, int n, int flags, uint32_t *d_moves,
                     int32_t *d_counts, cudaStream_t s) {
-  const int qs = flags & 1, gen = (flags >> 1) & 3;
-  if (gen == 2) return warp_genmoves_launch(d_boards, d_stm, n, qs, d_moves, d_counts, s);
+  const int qs = flags & 1, gen = (flags >> 1) & 3, allp = (flags >> 3) & 1;
   if (gen > 2) return set_error(ZETA_ERR_ARG, "genmoves: unknown generator");
-  k_genmoves<<<(n + 127) / 128, 128, 0, s>>>(d_boards, d_stm, n, qs, gen, d_moves, d_counts);
+  if (allp && gen != 0) return set_error(ZETA_ERR_ARG, "genmoves: all promotions only with the perft generator");
+  if (gen == 2) return warp_genmoves_launch(d_boards, d_stm, n, qs, d_moves, d_counts, s);
+  k_genmoves<<<(n + 127) / 128, 128, 0, s>>>(d_boards, d_stm, n, qs, gen, allp, d_moves, d_counts);
   ZCHECK(cudaGetLastError());
   ZCHECK(cudaStreamSynchronize(s));
   return ZETA_OK;
@@ -628,7 +647,7 @@ extern "C" int zeta_perft_batch_noalloc(const uint64_t *d_boards, const uint8_t 
       ZCHECK(cudaGetSymbolAddress(&p, g_noalloc_scratch));
       int nsm = 0, bps = 0;
       ZCHECK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-      ZCHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_perft_ws<128, 1>, 128, 0));
+      ZCHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_perft_ws<128, 1, false>, 128, 0));
       int nb = nsm * (bps > 0 ? bps : 1);
       if (nb > kNoAllocMaxBlocks) nb = kNoAllocMaxBlocks;
       g_noalloc_sms[dev] = nsm;
@@ -643,15 +662,18 @@ extern "C" int zeta_perft_batch_noalloc(const uint64_t *d_boards, const uint8_t 
   /* the array keeps the previous call's contents: clear what must start at zero */
   ZCHECK(cudaMemsetAsync(&S->pc, 0, sizeof(PerftCounters), s));
   ZCHECK(cudaMemsetAsync(S->cursors, 0, blocks * sizeof(uint32_t), s));
+  const bool allp = ctx().perft_allp != 0;
   k_roots<<<(n + 127) / 128, 128, 0, s>>>(d_boards, d_stm, d_depth, n, S->lvl[0], d_leaves, &S->pc);
   ZCHECK(cudaGetLastError());
+  const SplitKernel split = split_kernel(allp);
   for (int lv = 0; lv < kMaxLevels; lv++) {
-    k_split<<<sms * 4, 128, 0, s>>>(lv, S->lvl[lv & 1], S->lvl[(lv + 1) & 1], S->fin, kNoAllocMaxTasks,
-                                    kNoAllocMaxTasks, 0u, 3, &S->pc);
+    split<<<sms * 4, 128, 0, s>>>(lv, S->lvl[lv & 1], S->lvl[(lv + 1) & 1], S->fin, kNoAllocMaxTasks,
+                                  kNoAllocMaxTasks, 0u, 3, &S->pc);
     ZCHECK(cudaGetLastError());
   }
-  k_perft_ws<128, 1><<<blocks, 128, 0, s>>>(S->fin, S->cursors, d_leaves, &S->pc, S->nodes, 0u,
-                                            kNoAllocNodesPerBlock, kNoAllocMaxTasks, (uint32_t)n);
+  const WsKernel ws = ws_kernel(128, 1, allp);
+  ws<<<blocks, 128, 0, s>>>(S->fin, S->cursors, d_leaves, &S->pc, S->nodes, 0u, kNoAllocNodesPerBlock,
+                            kNoAllocMaxTasks, (uint32_t)n);
   ZCHECK(cudaGetLastError());
   uint32_t status = 0;
   ZCHECK(cudaMemcpyAsync(&status, &S->pc.status, sizeof status, cudaMemcpyDeviceToHost, s));

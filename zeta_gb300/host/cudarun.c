@@ -19,6 +19,7 @@
 
 static int g_inited = 0;
 static int g_pure = 0;
+static int g_all_promotions = 0;
 
 /* print_debug, src/clrun.c:1492-1506 */
 static clrun_bool fail(const char *what) {
@@ -28,6 +29,11 @@ static clrun_bool fail(const char *what) {
 }
 
 void cl_set_pure_search(int on) { g_pure = on != 0; }
+
+void cl_set_all_promotions(int on) {
+  g_all_promotions = on != 0;
+  if (g_inited) zeta_perft_set_promotions(g_all_promotions);
+}
 
 clrun_bool cl_init_device(char *kernelname) {
   if (g_inited) cl_release_device();
@@ -39,6 +45,7 @@ clrun_bool cl_init_device(char *kernelname) {
    * them from zeroed host images (src/clrun.c:404-443) */
   if (zeta_init(opencl_device_id, tt1_memory, tt2_memory) != ZETA_OK) return fail("zeta_init");
   g_inited = 1;
+  if (zeta_perft_set_promotions(g_all_promotions) != ZETA_OK) return fail("zeta_perft_set_promotions");
   return 1;
 }
 

@@ -2,7 +2,8 @@
  * main.c -- the zeta host binary (src/zeta.c:525-709): options, config,
  * device start-up, then the xboard command loop.
  *
- *   zeta [-s|--selftest] [-l|--log] [-p|--pure] [-d <device>] [-c <config.txt>] [-v] [-h]
+ *   zeta [-s|--selftest] [-l|--log] [-p|--pure] [-u|--allpromotions] [-d <device>] [-c <config.txt>]
+ *        [-v] [-h]
  */
 #include <stdlib.h>
 #include <string.h>
@@ -16,6 +17,8 @@ static void usage(void) {
          "  -l, --log        append a log to zeta.log\n"
          "  -p, --pure       pure fixed-depth alpha-beta (root score = negamax) instead of\n"
          "                   the reference's search with its heuristics\n"
+         "  -u, --allpromotions  perft promotes to queen, rook, bishop or knight (the\n"
+         "                   reference, and the default, promotes to a queen only)\n"
          "  -d <n>           CUDA device (default 0)\n"
          "  -c <file>        config file (default config.txt: threadsX, threadsY, tt1_memory, ...)\n"
          "  --guessconfig    measure the search on the device, write config.txt and exit\n"
@@ -42,6 +45,8 @@ int main(int argc, char **argv) {
       run_selftest = true;
     } else if (!strcmp(argv[i], "-p") || !strcmp(argv[i], "--pure")) {
       cl_set_pure_search(1);
+    } else if (!strcmp(argv[i], "-u") || !strcmp(argv[i], "--allpromotions")) {
+      cl_set_all_promotions(1);
     } else if (!strcmp(argv[i], "-l") || !strcmp(argv[i], "--log")) {
       LogFile = fopen("zeta.log", "a");
     } else if (!strcmp(argv[i], "-d") && i + 1 < argc) {

@@ -160,6 +160,14 @@ void xboard(void) {
       double s = (get_time_ms() - t0 + 1) / 1000.0;
       printf("nodecount:%" PRIu64 ", seconds: %lf, nps: %" PRIu64 " \n", ABNODECOUNT, s, (uint64_t)(ABNODECOUNT / s));
       if (!cl_release_device() || !cl_init_device("alphabeta_gpu")) exit(EXIT_FAILURE);
+    } else if (!strcmp(cmd, "promotions") && !xboard_mode) {
+      /* promotions all|queen: the promotion rule of the perft command
+       * (queen only is the reference's, and the default) */
+      char rule[16] = {0};
+      sscanf(arg, "%15s", rule);
+      if (!strcmp(rule, "all")) cl_set_all_promotions(1);
+      else if (!strcmp(rule, "queen")) cl_set_all_promotions(0);
+      else printf("Error (usage: promotions all|queen)\n");
     } else if (!strcmp(cmd, "selftest") && !xboard_mode) {
       selftest();
     } else if (!strcmp(cmd, "benchsmp") && !xboard_mode) {
@@ -185,6 +193,7 @@ void xboard(void) {
     } else if (!strcmp(cmd, "help") && !xboard_mode) {
       printf("# commands: new, setboard <fen>, go, usermove <move>, force, sd <depth>, st <seconds>,\n"
              "# level <moves> <minutes> <increment>, time <centiseconds>, perft <depth>,\n"
+             "# promotions all|queen (perft's promotion rule),\n"
              "# benchfile <file of FENs> [max workers],\n"
              "# benchsmp [max workers], selftest, print, quit (and the xboard protocol)\n");
     } else if (!strcmp(cmd, "accepted") || !strcmp(cmd, "rejected") || !strcmp(cmd, "random") ||
