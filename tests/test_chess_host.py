@@ -23,6 +23,13 @@ ROOTS = [
     ("rnbq1k1r/pp1Pbppp/2p5/8/2B5/8/PPP1NnPP/RNBQK2R w KQ - 1 8", 3),
     ("4k3/8/8/8/8/8/8/4K2R w K - 0 1", 5),
     ("7k/5Q2/6K1/8/8/8/8/8 b - - 0 1", 3),
+    # promotions: two pawns taking the same piece on the last rank, pushes,
+    # a check blocked by a promotion, a pinned pawn
+    ("2r4k/1P1P4/8/8/8/8/8/4K3 w - - 0 1", 3),
+    ("4k3/8/8/8/8/8/1p1p4/2R3K1 b - - 0 1", 3),
+    ("4k3/1P4P1/8/8/8/8/1p4p1/4K3 w - - 0 1", 4),
+    ("K6r/2P5/8/8/8/8/8/3k4 w - - 0 1", 4),
+    ("8/8/8/8/8/k7/1p6/2B4K b - - 0 1", 4),
 ]
 
 

@@ -104,3 +104,14 @@ def test_oracle_reproduces_workload_fixture_sample():
     assert sample
     for i in sample:
         assert ol.perft(boards[i], stm[i], 3, all_promotions=True) == fx["leaves"][i], i
+
+
+def test_two_pawns_promoting_on_the_same_square():
+    """Two pawns that can take the same piece on the last rank make two
+    capture promotions of each kind (eight moves, not four)."""
+    for fen in ("2r4k/1P1P4/8/8/8/8/8/4K3 w - - 0 1", "4k3/8/8/8/8/8/1p1p4/2R3K1 b - - 0 1"):
+        b, s = ol.setboard(fen)
+        caps = [m for m in ol.genmoves(b, s, qs=True, all_promotions=True) if ((m >> 18) & 15) >> 1 == 1]
+        assert len(caps) == 8 and len({m & 63 for m in caps}) == 2, fen
+        for d in range(1, 4):
+            assert mb.board_perft(b, s, d, True) == ol.perft(b, s, d, all_promotions=True), (fen, d)

@@ -111,6 +111,19 @@ def test_hand_made_promotion_positions(all_promotions):
         assert [int(x) for x in got] == row["all_promotions"], row["fen"]
 
 
+# two pawns that can take the same piece on the last rank: the bulk count
+# must count both captures (a union of the two capture sets counts one)
+DOUBLE_CAPTURE = ["2r4k/1P1P4/8/8/8/8/8/4K3 w - - 0 1", "4k3/8/8/8/8/8/1p1p4/2R3K1 b - - 0 1"]
+
+
+def test_two_pawns_promoting_on_the_same_square(all_promotions):
+    z = all_promotions
+    for fen in DOUBLE_CAPTURE:
+        b, s = ol.setboard(fen)
+        got = z.perft_batch(np.tile(b, (4, 1)), np.full(4, s, np.uint8), np.arange(1, 5, dtype=np.uint8))
+        assert [int(x) for x in got] == [ol.perft(b, s, d, all_promotions=True) for d in range(1, 5)], fen
+
+
 def test_noalloc_entry_follows_the_rule(all_promotions):
     torch = pytest.importorskip("torch")
     z = all_promotions

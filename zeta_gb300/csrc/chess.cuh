@@ -351,7 +351,13 @@ ZHD int count_legal_ex(const Pos &p, int stm, bool &in_check) {
   }
   n += popc(s1 & g.cmask) + popc(s2 & g.cmask) + popc(c1 & s.them & g.cmask) +
        popc(c2 & s.them & g.cmask);
-  if (ALLP) n += 3 * popc((s1 | ((c1 | c2) & s.them)) & g.cmask & (stm ? ZETA_RANK1 : ZETA_RANK8));
+  if (ALLP) {
+    /* pushes land on empty squares, captures on enemy ones: s1 and c1 are
+     * disjoint, but c1 and c2 may share a square (two pawns taking the same
+     * piece), so c2 is counted on its own */
+    const u64 last = g.cmask & (stm ? ZETA_RANK1 : ZETA_RANK8);
+    n += 3 * (popc((s1 | (c1 & s.them)) & last) + popc(c2 & s.them & last));
+  }
   u64 N = s.knights & s.us & free_;
   n += popc(((N << 17) & ZETA_NOTA) & tgt) + popc(((N << 15) & ZETA_NOTH) & tgt) +
        popc(((N << 10) & ZETA_NOTAB) & tgt) + popc(((N << 6) & ZETA_NOTGH) & tgt) +

@@ -671,7 +671,9 @@ extern "C" int zeta_perft_batch_noalloc(const uint64_t *d_boards, const uint8_t 
                                   kNoAllocMaxTasks, 0u, 3, &S->pc);
     ZCHECK(cudaGetLastError());
   }
-  const WsKernel ws = ws_kernel(128, 1, allp);
+  /* blocks_per_sm 0 names the uncapped variant, k_perft_ws<128, 1, allp> */
+  const WsKernel ws = ws_kernel(128, 0, allp);
+  if (!ws) return set_error(ZETA_ERR_ARG, "no perft kernel variant for the allocation-free entry");
   ws<<<blocks, 128, 0, s>>>(S->fin, S->cursors, d_leaves, &S->pc, S->nodes, 0u, kNoAllocNodesPerBlock,
                             kNoAllocMaxTasks, (uint32_t)n);
   ZCHECK(cudaGetLastError());
