@@ -78,13 +78,13 @@ int zeta_perft_batch_device(const uint64_t *d_boards, const uint8_t *d_stm, cons
  *    131072 subtree tasks per level; beyond either it returns
  *    ZETA_ERR_NOALLOC.
  *  - The first call on a device looks up the array's device address (its
- *    host-side name is not a device address); make that first call before
- *    any stream capture.  That one-time set-up is serialised between host
- *    threads.
+ *    host-side name is not a device address); that one-time set-up is
+ *    serialised between host threads.
  *  - All calls share the one array: calls that overlap on the GPU (other
  *    streams, other host threads) race and give wrong counts.  Every call
  *    copies a status word back and synchronises `stream` before it
- *    returns. */
+ *    returns, so a call cannot be captured into a CUDA graph.
+ *  - Promotions follow zeta_perft_set_promotions, like the other entries. */
 int zeta_perft_batch_noalloc(const uint64_t *d_boards, const uint8_t *d_stm, const uint8_t *d_depth, int n,
                              uint64_t *d_leaves, void *stream);
 
