@@ -376,13 +376,16 @@ def search_batch_block(z, local, rank, args):
     torch.cuda.synchronize()
     steps = 3
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
-    kms, nodes = [], 0
+    kms, nodes, probes, stores = [], 0, 0, 0
     with ClockSampler(local) as clocks:
         for a, b in ev:
             a.record(stream)
             step()
             b.record(stream)
             kms.append(z.search_last_ms())
+            pr, sto = z.search_last_table_ops()
+            probes += pr
+            stores += sto
             nodes += int(d_nd.sum().item())
         torch.cuda.synchronize()
     ms = [a.elapsed_time(b) for a, b in ev]
@@ -392,6 +395,15 @@ def search_batch_block(z, local, rank, args):
     total_s = sum(ms) / 1e3
     nps = nodes / total_s
     roofline = _node_roofline(z, nps, "ops_per_search_node", "k_search_warp" if s_form == 3 else "k_search_pure")
+    # the table's traffic, counted on the device: one 32-byte sector per
+    # probe or store, against the measured HBM copy bandwidth
+    tt_bytes = 32 * (probes + stores) / steps
+    hbm = measured_peaks().get("hbm_gbs")
+    tt_gbs = tt_bytes / (sum(kms) / len(kms) / 1e3) / 1e9
+    table = {"probes_per_step": probes // steps, "stores_per_step": stores // steps,
+             "bytes_per_step": int(tt_bytes), "gbs": round(tt_gbs, 2), "hbm_peak_gbs": hbm,
+             "frac_of_hbm": round(tt_gbs / hbm, 4) if hbm else None,
+             "rule": "32 B sector per 16-byte entry probed or stored, counted on the device"}
     z.release()
     cpu, vals = (None, None) if args.no_cpu else oracle_search_sample(boards, stm, depth)
     if vals is not None and list(scores[:len(vals)]) != [int(v) for v in vals]:
@@ -406,7 +418,7 @@ def search_batch_block(z, local, rank, args):
                    "helper_cap": s_helpers, "tt": "1 GiB, 16-byte entries, cleared every step",
                    "l2": "the 1 GiB table and 2.4 G node visits per step exceed L2"},
         "nodes_per_s": round(nps, 1), "nodes_per_step": nodes // steps,
-        "roofline": roofline,
+        "roofline": roofline, "table_traffic": table,
         "oracle_cpu": cpu, "scores_checked_against_oracle": 0 if vals is None else len(vals),
         "clocks": clocks.summary(), "gpu_launches": steps * 3,
     }

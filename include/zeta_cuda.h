@@ -198,6 +198,13 @@ int zeta_engine_set_helper_depth(int every);
 int zeta_tt_clear(void);
 /* device time of the last search kernel, ms */
 int zeta_search_last_ms(float *kernel_ms);
+/* Transposition-table operations of the last batched pure search, counted
+ * on the device: probes (one per interior node entered and per depth-1
+ * child looked up) and stores (one per finished node).  Each touches one
+ * 16-byte entry in one 32-byte DRAM sector, so 32 B x (probes + stores)
+ * is the table's traffic (the reference's per-node TT1 load and store,
+ * zeta.cl:1623 and 1894-1913). */
+int zeta_search_last_table_ops(uint64_t *probes, uint64_t *stores);
 
 /* ------------------------------------------------------------------ */
 /* Full-engine search: the reference's alphabeta_gpu (zeta.cl:852-2511)

@@ -99,6 +99,11 @@ def test_launch_forms_give_the_same_scores(zeta_device, form):
             scores, moves, nodes = z.search_batch(boards, stm, 4, workers)
             assert list(scores) == want, (form, workers)
             assert (nodes > 0).all()
+            # table operations counted on the device: each node entered
+            # probes at most once and each finished node stores once
+            probes, stores = z.search_last_table_ops()
+            assert 0 < stores <= probes + len(stm) * workers and probes + stores <= 2 * int(nodes.sum()), \
+                (form, workers, probes, stores, int(nodes.sum()))
     finally:
         z.search_set_launch_form(0)
 

@@ -120,6 +120,7 @@ SIGNATURES = {
     "zeta_search_set_launch_form": (ctypes.c_int, [ctypes.c_int]),
     "zeta_engine_set_helper_depth": (ctypes.c_int, [ctypes.c_int]),
     "zeta_search_last_ms": (ctypes.c_int, [ctypes.POINTER(ctypes.c_float)]),
+    "zeta_search_last_table_ops": (ctypes.c_int, [_u64p, _u64p]),
     "zeta_genmoves_batch": (ctypes.c_int, [_u64p, _u8p, ctypes.c_int, ctypes.c_int, _u32p, _i32p]),
     "zeta_eval_batch": (ctypes.c_int, [_u64p, ctypes.c_int, _i32p]),
 }
@@ -418,6 +419,13 @@ def search_last_ms() -> float:
     t = ctypes.c_float()
     _check(load_library().zeta_search_last_ms(ctypes.byref(t)))
     return t.value
+
+
+def search_last_table_ops() -> tuple[int, int]:
+    """(probes, stores) of the transposition table in the last batched search."""
+    a, b = ctypes.c_uint64(), ctypes.c_uint64()
+    _check(load_library().zeta_search_last_table_ops(ctypes.byref(a), ctypes.byref(b)))
+    return a.value, b.value
 
 
 def int_peak_tops() -> float:

@@ -389,6 +389,13 @@ int zeta_tt_clear(void) {
   return ZETA_OK;
 }
 
+int zeta_search_last_table_ops(uint64_t *probes, uint64_t *stores) {
+  if (!probes || !stores) return set_error(ZETA_ERR_ARG, "null pointer");
+  *probes = g_ctx.s_probes;
+  *stores = g_ctx.s_stores;
+  return ZETA_OK;
+}
+
 int zeta_search_last_ms(float *kernel_ms) {
   if (!kernel_ms) return set_error(ZETA_ERR_ARG, "null pointer");
   *kernel_ms = g_ctx.sstats.kernel_ms;

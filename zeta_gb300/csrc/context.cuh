@@ -109,6 +109,7 @@ struct Context {
   uint32_t *s_busy = nullptr; /* ABDADA busy table */
   uint64_t s_busy_entries = 0;
   uint32_t *s_status = nullptr;
+  unsigned long long s_probes = 0, s_stores = 0; /* table operations of the last batched search */
   int s_helpers_cap = 0;      /* max workers per position once helpers join; 0 = no helpers */
   int s_launch_form = 0;      /* search kernels: 0 auto, 1 dense, 2 sparse, 3 warp (pure search) */
   int e_deep_every = 0;       /* full engine, lazy SMP: every k-th helper one ply deeper (0 = off) */

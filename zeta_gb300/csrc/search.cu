@@ -54,6 +54,7 @@ constexpr int kMate = 30000;            /* MATESCORE */
 constexpr int kOnEval = 32500;          /* "searched by another worker" */
 constexpr int kMaxSearchDepth = 16;
 constexpr int kMaxMoves = 218;
+constexpr size_t kSearchStatusBytes = 24; /* status word, pad, table probes (u64), table stores (u64) */
 constexpr int kAbdadaMinDepth = 2;
 constexpr uint32_t kDone = 1u << 30;    /* move flags above the 30-bit packing */
 constexpr uint32_t kDefer = 1u << 31;
@@ -178,6 +179,7 @@ struct Worker {
   u64 busy_mask;
   const EvalTables *T;
   unsigned long long nodes, tthits;
+  unsigned long long probes, stores; /* table operations over the worker's life */
   Move killer[kMaxSearchDepth + 1][2];
   int scores[kMaxMoves];
   /* learned ordering */
@@ -218,6 +220,7 @@ __device__ bool node_enter(Worker &W, Frame &f, int ply, int &value) {
   Move ttm = 0;
   int ts, td, tb;
   Move tm;
+  W.probes++;
   if (tt_probe(W.tt, W.tt_mask, f.key, ts, td, tb, tm)) {
     ttm = tm; /* a move from any depth orders; only an equal depth cuts */
     if (td == f.depth) {
@@ -313,6 +316,7 @@ __device__ bool node_enter(Worker &W, Frame &f, int ply, int &value) {
 __device__ __forceinline__ int node_finish(Worker &W, Frame &f, int ply) {
   if (f.busy) atomicSub(&W.busy[(f.key >> 32) & W.busy_mask], 1u);
   int bound = f.best <= f.alpha0 ? B_UPPER : (f.best >= f.beta ? B_LOWER : B_EXACT);
+  W.stores++;
   tt_store(W.tt, W.tt_mask, f.key, to_tt(f.best, ply), f.depth, bound, f.bestmove);
   return f.best;
 }
@@ -322,7 +326,8 @@ __global__ void __launch_bounds__(TPB) k_search_pure(const uint64_t *__restrict_
                                                      int N, int nworkers, int depth, TTEntry *tt, u64 tt_mask,
                                                      uint32_t *busy, u64 busy_mask, uint32_t *done, SearchOut *out,
                                                      unsigned long long budget, uint32_t *status, uint32_t *active,
-                                                     int max_per_pos, LearnArgs la, int sparse) {
+                                                     int max_per_pos, LearnArgs la, int sparse,
+                                                     unsigned long long *ttops) {
   __shared__ EvalTables sT;
   for (int i = threadIdx.x; i < (int)(sizeof(EvalTables) / 4); i += TPB)
     ((uint32_t *)&sT)[i] = ((const uint32_t *)&kEvalDev)[i];
@@ -352,6 +357,7 @@ __global__ void __launch_bounds__(TPB) k_search_pure(const uint64_t *__restrict_
   W.oreq = la.req;
   W.noreq = la.nreq;
   W.oreq_cap = la.cap;
+  W.probes = W.stores = 0;
   unsigned long long steps = 0;
 
   /* A worker searches its own position, then helps unfinished ones: it
@@ -486,6 +492,8 @@ __global__ void __launch_bounds__(TPB) k_search_pure(const uint64_t *__restrict_
     atomicAdd(&out[p].tthits, W.tthits);
     atomicSub(&active[p], 1u);
   }
+  atomicAdd(ttops, W.probes);
+  atomicAdd(ttops + 1, W.stores);
 }
 
 /* Hand-off from a warp's tree walker (lane 0) to all 32 lanes: a node with
@@ -736,6 +744,7 @@ __device__ bool wnode_pre(Worker &W, WFrame &f, int ply, int &value, WarpGen &G)
   Move ttm = 0;
   int ts, td, tb;
   Move tm;
+  W.probes++;
   if (tt_probe(W.tt, W.tt_mask, f.key, ts, td, tb, tm)) {
     ttm = tm;
     if (td == f.depth) {
@@ -813,6 +822,7 @@ __device__ bool wnode_post(Worker &W, WFrame &f, int ply, const Move *srt, int n
 __device__ __forceinline__ int wnode_finish(Worker &W, WFrame &f, int ply) {
   if (f.busy) atomicSub(&W.busy[(f.key >> 32) & W.busy_mask], 1u);
   const int bound = f.best <= f.alpha0 ? B_UPPER : (f.best >= f.beta ? B_LOWER : B_EXACT);
+  W.stores++;
   tt_store(W.tt, W.tt_mask, f.key, to_tt(f.best, ply), f.depth, bound, f.bestmove);
   return f.best;
 }
@@ -838,7 +848,7 @@ __global__ void __launch_bounds__(TPB, 4) k_search_warp(const uint64_t *__restri
                                                      int N, int nworkers, int depth, TTEntry *tt, u64 tt_mask,
                                                      uint32_t *busy, u64 busy_mask, uint32_t *done, SearchOut *out,
                                                      unsigned long long budget, uint32_t *status, uint32_t *active,
-                                                     int max_per_pos, LearnArgs la) {
+                                                     int max_per_pos, LearnArgs la, unsigned long long *ttops) {
   __shared__ EvalTables sT;
   __shared__ LeafBatch LB[TPB / 32];
   __shared__ WarpGen WG[TPB / 32];
@@ -866,6 +876,7 @@ __global__ void __launch_bounds__(TPB, 4) k_search_warp(const uint64_t *__restri
   W.oreq = la.req;
   W.noreq = la.nreq;
   W.oreq_cap = la.cap;
+  W.probes = W.stores = 0;
   unsigned long long steps = 0;
   int p = (int)(t % N), job = 0, ply = 0;
   int phase = 0; /* lane 0: 0 take a job, 1 walk, 2 take a batch's value, 3 finish a node entry */
@@ -989,6 +1000,7 @@ __global__ void __launch_bounds__(TPB, 4) k_search_warp(const uint64_t *__restri
           } else {
             const Move bm = B.moves[bidx];
             if (pend == 2) {
+              W.stores++;
               tt_store(W.tt, W.tt_mask, F[0].key, bval, 1, B_EXACT, bm);
               if (atomicCAS(&done[p], 0u, 1u) == 0u) {
                 out[p].score = bval;
@@ -1000,6 +1012,7 @@ __global__ void __launch_bounds__(TPB, 4) k_search_warp(const uint64_t *__restri
               phase = 0;
               continue;
             }
+            W.stores++;
             tt_store(W.tt, W.tt_mask, F[ply + 1].key, to_tt(bval, ply + 1), 1, bdone == B.n ? B_EXACT : B_LOWER,
                      bm);
             val = -bval;
@@ -1055,6 +1068,7 @@ __global__ void __launch_bounds__(TPB, 4) k_search_warp(const uint64_t *__restri
               int ts, td, tb;
               Move tm;
               bool hit = false;
+              W.probes++;
               if (tt_probe(W.tt, W.tt_mask, g.key, ts, td, tb, tm) && td == 1) {
                 const int s = from_tt(ts, ply + 1);
                 if (tb == B_EXACT || (tb == B_LOWER && s >= g.beta) || (tb == B_UPPER && s <= g.alpha)) {
@@ -1156,6 +1170,10 @@ __global__ void __launch_bounds__(TPB, 4) k_search_warp(const uint64_t *__restri
     bdone = scored;
     __syncwarp(); /* B is read by every lane before lane 0 writes it again */
   }
+  if (lane == 0) {
+    atomicAdd(ttops, W.probes);
+    atomicAdd(ttops + 1, W.stores);
+  }
 }
 
 /* the static evaluation (white's view) of n boards, for the parity test */
@@ -1202,7 +1220,8 @@ static int search_buffers(int n) {
     c.s_busy_entries = 1ull << 22;
     ZCHECK(cudaMalloc(&c.s_busy, c.s_busy_entries * sizeof(uint32_t)));
   }
-  if (!c.s_status) ZCHECK(cudaMalloc(&c.s_status, sizeof(uint32_t)));
+  /* status word, then (8-byte aligned) the table probes and stores */
+  if (!c.s_status) ZCHECK(cudaMalloc(&c.s_status, kSearchStatusBytes));
   if (!c.tt1 && !c.s_tt) {
     c.s_tt_entries = 1ull << 22; /* 64 MiB of 16-byte entries */
     ZCHECK(cudaMalloc(&c.s_tt, c.s_tt_entries * sizeof(TTEntry)));
@@ -1273,7 +1292,8 @@ int search_pure_launch(const uint64_t *d_boards, const uint8_t *d_stm, int n, in
   ZCHECK(cudaMemsetAsync(c.s_out, 0, (size_t)n * sizeof(SearchOut), s));
   ZCHECK(cudaMemsetAsync(c.s_done, 0, (size_t)2 * n * sizeof(uint32_t), s));
   ZCHECK(cudaMemsetAsync(c.s_busy, 0, c.s_busy_entries * sizeof(uint32_t), s));
-  ZCHECK(cudaMemsetAsync(c.s_status, 0, sizeof(uint32_t), s));
+  ZCHECK(cudaMemsetAsync(c.s_status, 0, kSearchStatusBytes, s));
+  unsigned long long *ttops = (unsigned long long *)(c.s_status + 2);
   const long long total = (long long)n * workers;
   const int tpb = 128;
   /* automatic form: warp-cooperative when every worker can have a resident
@@ -1294,18 +1314,21 @@ int search_pure_launch(const uint64_t *d_boards, const uint8_t *d_stm, int n, in
   if (form == 3)
     k_search_warp<128><<<blocks, tpb, 0, s>>>(d_boards, d_stm, n, workers, depth, tt, entries - 1, c.s_busy,
                                               c.s_busy_entries - 1, c.s_done, (SearchOut *)c.s_out, budget,
-                                              c.s_status, c.s_done + n, c.s_helpers_cap, la);
+                                              c.s_status, c.s_done + n, c.s_helpers_cap, la, ttops);
   else
     k_search_pure<128><<<blocks, tpb, 0, s>>>(d_boards, d_stm, n, workers, depth, tt, entries - 1, c.s_busy,
                                               c.s_busy_entries - 1, c.s_done, (SearchOut *)c.s_out, budget,
-                                              c.s_status, c.s_done + n, c.s_helpers_cap, la, form == 2);
+                                              c.s_status, c.s_done + n, c.s_helpers_cap, la, form == 2, ttops);
   ZCHECK(cudaGetLastError());
   ZCHECK(cudaEventRecord(c.ev[2], s));
   k_search_scatter<<<(n + 127) / 128, 128, 0, s>>>((const SearchOut *)c.s_out, n, d_scores, d_moves, d_nodes);
   ZCHECK(cudaGetLastError());
-  uint32_t status = 0;
-  ZCHECK(cudaMemcpyAsync(&status, c.s_status, 4, cudaMemcpyDeviceToHost, s));
+  uint32_t st[kSearchStatusBytes / 4] = {0};
+  ZCHECK(cudaMemcpyAsync(st, c.s_status, kSearchStatusBytes, cudaMemcpyDeviceToHost, s));
   ZCHECK(cudaStreamSynchronize(s));
+  const uint32_t status = st[0];
+  memcpy(&c.s_probes, st + 2, 8);
+  memcpy(&c.s_stores, st + 4, 8);
   float ms = -1.f;
   if (cudaEventElapsedTime(&ms, c.ev[1], c.ev[2]) != cudaSuccess) ms = -1.f;
   (void)cudaGetLastError();
