@@ -89,3 +89,32 @@ def test_gemm_fp8_matches_fp32(zeta_device, m, n, k):
     torch.cuda.synchronize()
     ref = a.float() @ b.float().T
     _check(torch, c, ref)
+
+
+@pytest.mark.parametrize("m,n,k,fp8", [(65536, 512, 768, False), (20000, 384, 256, False), (65536, 256, 512, True),
+                                       (40000, 48, 128, False)])
+def test_persistent_gemm_many_tiles_per_cta(zeta_device, m, n, k, fp8):
+    """Shapes with many more output tiles than SMs, so that every CTA of
+    the persistent kernel runs several tiles through both tensor-memory
+    accumulators and its ring of K slices runs on from tile to tile (M and
+    N not multiples of the tile for two of them).  Against FP32, and bit
+    for bit against the per-tile kernel (the same MMAs per tile in the
+    same order)."""
+    torch = pytest.importorskip("torch")
+    z = zeta_device
+    g = torch.Generator(device="cuda").manual_seed(m + 3 * n + 7 * k)
+    dt = torch.float8_e4m3fn if fp8 else torch.bfloat16
+    a = torch.randn(m, k, device="cuda", generator=g).to(dt)
+    b = torch.randn(n, k, device="cuda", generator=g).to(dt)
+    out = {}
+    try:
+        for mode in (3, 1):
+            z.gemm_configure(mode)
+            c = torch.full((m, n), float("nan"), device="cuda")
+            z.gemm_tc(a.data_ptr(), b.data_ptr(), c.data_ptr(), m, n, k, fp8=fp8)
+            torch.cuda.synchronize()
+            out[mode] = c
+    finally:
+        z.gemm_configure(0)
+    _check(torch, out[3], a.float() @ b.float().T)
+    assert torch.equal(out[3], out[1])

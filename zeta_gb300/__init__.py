@@ -269,6 +269,7 @@ def search_set_launch_form(form: int) -> None:
 
 
 def gemm_configure(ctas_per_sm: int) -> None:
+    """0 automatic (persistent), 1 / 2 per-tile kernel with its ring for 1 / 2 CTAs per SM, 3 persistent."""
     _check(load_library().zeta_gemm_configure(ctas_per_sm))
 
 

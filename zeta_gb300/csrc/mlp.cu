@@ -26,6 +26,7 @@
 #include <cuda_bf16.h>
 #include <cuda_fp8.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <vector>
@@ -74,6 +75,77 @@ struct GemmArgs {
  * bounded: a timeout sets an error word, the producer's copies still in
  * flight are awaited (bounded), tensor memory is freed. */
 constexpr int kMaxStages = 8;
+
+/* Epilogue of one 128 x BN accumulator: the calling warp's 32 TMEM lanes
+ * (tacc addresses lane 0 of them and the accumulator's first column) are
+ * rows row..row of C (one row per thread); scale, bias, ReLU, ReLU mask,
+ * then the FP32 / BF16 / transposed BF16 stores (atomic FP32 adds when the
+ * K range was split across CTAs). */
+template <int BN>
+__device__ __forceinline__ void gemm_epilogue(const GemmArgs &g, uint32_t tacc, int row, int n0, float scale,
+                                              bool split) {
+#pragma unroll 1
+  for (int c0 = 0; c0 < BN; c0 += 16) {
+    float v[16];
+    tc::tmem_ld16(tacc + (uint32_t)c0, v);
+    const int cb = n0 + c0;
+    if (row >= g.M || cb >= g.N) continue;
+    const bool whole = cb + 16 <= g.N;
+#pragma unroll
+    for (int j = 0; j < 16; j++) {
+      float x = v[j] * scale;
+      if (g.bias && cb + j < g.N) x += g.bias[cb + j];
+      if (g.relu) x = fmaxf(x, 0.f);
+      v[j] = x;
+    }
+    if (g.mask) {
+      const bf16 *mk = g.mask + (size_t)row * g.N + cb;
+#pragma unroll
+      for (int j = 0; j < 16; j++)
+        if (cb + j < g.N && !(__bfloat162float(mk[j]) > 0.f)) v[j] = 0.f;
+    }
+    if (g.Cf) {
+      float *cp = g.Cf + (size_t)row * g.N + cb;
+      if (split) {
+#pragma unroll
+        for (int j = 0; j < 16; j++)
+          if (cb + j < g.N) atomicAdd(cp + j, v[j]);
+      } else if (whole && ((uintptr_t)cp & 15) == 0) {
+#pragma unroll
+        for (int j = 0; j < 16; j += 4) *(float4 *)(cp + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
+      } else {
+#pragma unroll
+        for (int j = 0; j < 16; j++)
+          if (cb + j < g.N) cp[j] = v[j];
+      }
+    }
+    if (g.Cb) {
+      bf16 *cp = g.Cb + (size_t)row * g.N + cb;
+      if (whole && ((uintptr_t)cp & 15) == 0) {
+        __align__(16) bf16 h[16];
+#pragma unroll
+        for (int j = 0; j < 16; j++) h[j] = __float2bfloat16(v[j]);
+        *(uint4 *)cp = *(const uint4 *)h;
+        *(uint4 *)(cp + 8) = *(const uint4 *)(h + 8);
+      } else {
+#pragma unroll
+        for (int j = 0; j < 16; j++)
+          if (cb + j < g.N) cp[j] = __float2bfloat16(v[j]);
+      }
+    }
+    if (g.Ct) {
+#pragma unroll
+      for (int j = 0; j < 16; j++)
+        if (cb + j < g.N) g.Ct[(size_t)(cb + j) * g.M + row] = __float2bfloat16(v[j]);
+    }
+  }
+}
+
+__device__ __forceinline__ float gemm_scale(const GemmArgs &g) {
+  float scale = g.scale;
+  if (g.amaxA && g.amaxB) scale *= (__uint_as_float(*g.amaxA) / 448.f) * (__uint_as_float(*g.amaxB) / 448.f);
+  return scale;
+}
 
 template <int BN, bool FP8>
 __global__ void __launch_bounds__(128, 1)
@@ -149,66 +221,8 @@ __global__ void __launch_bounds__(128, 1)
   __syncthreads();
   tc::fence_after_sync();
   if (finished && !s_fail) {
-    float scale = g.scale;
-    if (g.amaxA && g.amaxB)
-      scale *= (__uint_as_float(*g.amaxA) / 448.f) * (__uint_as_float(*g.amaxB) / 448.f);
-    const int row = m0 + warp * 32 + lane;
-    const bool split = gridDim.z > 1;
-#pragma unroll 1
-    for (int c0 = 0; c0 < BN; c0 += 16) {
-      float v[16];
-      tc::tmem_ld16(taddr + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
-      const int cb = n0 + c0;
-      if (row >= g.M || cb >= g.N) continue;
-      const bool whole = cb + 16 <= g.N;
-#pragma unroll
-      for (int j = 0; j < 16; j++) {
-        float x = v[j] * scale;
-        if (g.bias && cb + j < g.N) x += g.bias[cb + j];
-        if (g.relu) x = fmaxf(x, 0.f);
-        v[j] = x;
-      }
-      if (g.mask) {
-        const bf16 *mk = g.mask + (size_t)row * g.N + cb;
-#pragma unroll
-        for (int j = 0; j < 16; j++)
-          if (cb + j < g.N && !(__bfloat162float(mk[j]) > 0.f)) v[j] = 0.f;
-      }
-      if (g.Cf) {
-        float *cp = g.Cf + (size_t)row * g.N + cb;
-        if (split) {
-#pragma unroll
-          for (int j = 0; j < 16; j++)
-            if (cb + j < g.N) atomicAdd(cp + j, v[j]);
-        } else if (whole && ((uintptr_t)cp & 15) == 0) {
-#pragma unroll
-          for (int j = 0; j < 16; j += 4) *(float4 *)(cp + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
-        } else {
-#pragma unroll
-          for (int j = 0; j < 16; j++)
-            if (cb + j < g.N) cp[j] = v[j];
-        }
-      }
-      if (g.Cb) {
-        bf16 *cp = g.Cb + (size_t)row * g.N + cb;
-        if (whole && ((uintptr_t)cp & 15) == 0) {
-          __align__(16) bf16 h[16];
-#pragma unroll
-          for (int j = 0; j < 16; j++) h[j] = __float2bfloat16(v[j]);
-          *(uint4 *)cp = *(const uint4 *)h;
-          *(uint4 *)(cp + 8) = *(const uint4 *)(h + 8);
-        } else {
-#pragma unroll
-          for (int j = 0; j < 16; j++)
-            if (cb + j < g.N) cp[j] = __float2bfloat16(v[j]);
-        }
-      }
-      if (g.Ct) {
-#pragma unroll
-        for (int j = 0; j < 16; j++)
-          if (cb + j < g.N) g.Ct[(size_t)(cb + j) * g.M + row] = __float2bfloat16(v[j]);
-      }
-    }
+    gemm_epilogue<BN>(g, taddr + ((uint32_t)(warp * 32) << 16), m0 + warp * 32 + lane, n0, gemm_scale(g),
+                      gridDim.z > 1);
   } else {
     if (tid == 0) {
       atomicOr(g.err, MST_TIMEOUT);
@@ -222,6 +236,157 @@ __global__ void __launch_bounds__(128, 1)
   tc::fence_before_sync();
   __syncthreads();
   if (warp == 0) tc::tmem_free(taddr, BN);
+}
+
+/* The same product as a persistent kernel: one CTA per SM walks the
+ * output tiles t = blockIdx.x, blockIdx.x + gridDim.x, ... (tile t is rows
+ * 128 (t / nt), columns BN (t % nt), so neighbouring CTAs share their A
+ * rows in L2), 192 threads:
+ *   warp 0, lane 0  TMA producer: K slices of every tile in turn into a
+ *                   ring of `stages` slots that runs on across tiles;
+ *   warp 1, lane 0  MMA issuer: tile j into tensor-memory accumulator
+ *                   j & 1 (two accumulators of BN columns), then
+ *                   tcgen05.commit on that accumulator's "full" barrier;
+ *   warps 2-5       epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31
+ *                   of the finished accumulator, stores the rows and
+ *                   releases the accumulator ("empty" barrier, one arrival
+ *                   per warp).
+ * So the epilogue of tile j runs under the MMAs of tile j + 1 and the
+ * loads of the tiles after it.  Every wait is bounded; a timeout sets an
+ * error word, every role stops, the producer's copies still in flight and
+ * the issued MMAs are awaited (bounded), and tensor memory is freed.  The
+ * launch asks for enough shared memory that two CTAs never share an SM,
+ * so the 2 x BN-column allocation never waits for another CTA. */
+constexpr int kPersistThreads = 192;
+
+template <int BN, bool FP8>
+__global__ void __launch_bounds__(kPersistThreads, 1)
+    k_gemm_persist(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, GemmArgs g,
+                   int stages) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t *base = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  constexpr uint32_t A_BYTES = 128 * 128, B_BYTES = BN * 128, STAGE = A_BYTES + B_BYTES;
+  __shared__ uint64_t full[kMaxStages], empty[kMaxStages], acc_full[2], acc_empty[2], done;
+  __shared__ uint32_t s_taddr;
+  __shared__ int s_fail;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  constexpr int EK = FP8 ? 128 : 64; /* K elements per 128-byte row */
+  constexpr uint32_t IDESC = FP8 ? tc::idesc_f8(128, BN) : tc::idesc_f16(128, BN, 1);
+  const int nkb = g.K / EK;
+  const int nt = (g.N + BN - 1) / BN;
+  const int ntiles = ((g.M + 127) / 128) * nt;
+
+  if (warp == 0) tc::tmem_alloc(&s_taddr, 2 * BN);
+  if (tid == 32) {
+    for (int i = 0; i < stages; i++) {
+      tc::mbar_init(&full[i], 1);
+      tc::mbar_init(&empty[i], 1);
+    }
+    for (int a = 0; a < 2; a++) {
+      tc::mbar_init(&acc_full[a], 1);
+      tc::mbar_init(&acc_empty[a], 4);
+    }
+    tc::mbar_init(&done, 1);
+    s_fail = 0;
+    tc::prefetch_tmap(&tmA);
+    tc::prefetch_tmap(&tmB);
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t taddr = s_taddr;
+  volatile int *fail = &s_fail;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      /* producer */
+      uint32_t it = 0;
+      bool ok = true;
+      for (int t = blockIdx.x; ok && t < ntiles; t += gridDim.x) {
+        const int m0 = (t / nt) * 128, n0 = (t % nt) * BN;
+        for (int kb = 0; kb < nkb; kb++) {
+          const uint32_t sl = it % (uint32_t)stages, use = it / (uint32_t)stages;
+          if ((use > 0 && !tc::mbar_wait(&empty[sl], (use - 1) & 1, kWaitTries)) || *fail) {
+            ok = false;
+            break;
+          }
+          uint8_t *sa = base + (size_t)sl * STAGE;
+          tc::mbar_arrive_expect_tx(&full[sl], STAGE);
+          tc::tma_load_2d(sa, &tmA, kb * EK, m0, &full[sl]);
+          tc::tma_load_2d(sa + A_BYTES, &tmB, kb * EK, n0, &full[sl]);
+          it++;
+        }
+      }
+      if (!ok) {
+        *fail = 1;
+        /* copies still in flight land before the memory goes away */
+        for (uint32_t i = it > (uint32_t)stages ? it - (uint32_t)stages : 0u; i < it; i++)
+          tc::mbar_wait(&full[i % (uint32_t)stages], (i / (uint32_t)stages) & 1, kWaitTries);
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      /* MMA issuer */
+      uint32_t it = 0;
+      bool ok = true;
+      int j = 0;
+      for (int t = blockIdx.x; ok && t < ntiles; t += gridDim.x, j++) {
+        const int a = j & 1;
+        if (j >= 2 && !tc::mbar_wait(&acc_empty[a], ((j >> 1) - 1) & 1, kWaitTries)) {
+          ok = false;
+          break;
+        }
+        tc::fence_after_sync();
+        const uint32_t tacc = taddr + (uint32_t)(a * BN);
+        for (int kb = 0; kb < nkb; kb++) {
+          const uint32_t sl = it % (uint32_t)stages;
+          if (!tc::mbar_wait(&full[sl], (it / (uint32_t)stages) & 1, kWaitTries) || *fail) {
+            ok = false;
+            break;
+          }
+          tc::fence_after_sync();
+          const uint32_t a0 = tc::smem_u32(base + (size_t)sl * STAGE), b0 = a0 + A_BYTES;
+#pragma unroll
+          for (int k = 0; k < 4; k++) {
+            const uint64_t ad = tc::smem_desc_sw128(a0 + 32 * k), bd = tc::smem_desc_sw128(b0 + 32 * k);
+            if (FP8) tc::mma_f8(tacc, ad, bd, IDESC, (kb > 0 || k > 0) ? 1u : 0u);
+            else tc::mma_f16(tacc, ad, bd, IDESC, (kb > 0 || k > 0) ? 1u : 0u);
+          }
+          tc::mma_commit(&empty[sl]);
+          it++;
+        }
+        if (!ok) break;
+        tc::mma_commit(&acc_full[a]); /* arrives when the tile's MMAs have completed */
+      }
+      if (!ok) *fail = 1;
+      tc::mma_commit(&done);
+      tc::mbar_wait(&done, 0, kWaitTries); /* every MMA issued above has completed */
+    }
+  } else {
+    /* epilogue: TMEM lanes 32 q .. 32 q + 31 are rows 32 q .. of the tile */
+    const int q = warp & 3;
+    const float scale = gemm_scale(g);
+    int j = 0;
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x, j++) {
+      const int a = j & 1;
+      const bool got = tc::mbar_wait(&acc_full[a], (j >> 1) & 1, kWaitTries);
+      /* warp-uniform decision: tcgen05.ld needs the whole warp */
+      if (!__all_sync(0xFFFFFFFFu, got) || __shfl_sync(0xFFFFFFFFu, *fail, 0)) {
+        if (lane == 0) *fail = 1;
+        break;
+      }
+      tc::fence_after_sync();
+      gemm_epilogue<BN>(g, taddr + ((uint32_t)(q * 32) << 16) + (uint32_t)(a * BN), (t / nt) * 128 + q * 32 + lane,
+                        (t % nt) * BN, scale, false);
+      tc::fence_before_sync();
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive(&acc_empty[a]);
+    }
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (tid == 0 && *fail) atomicOr(g.err, MST_TIMEOUT);
+  if (warp == 0) tc::tmem_free(taddr, 2 * BN);
 }
 
 /* driver's tensor-map encoder, looked up once through the runtime */
@@ -257,15 +422,18 @@ int make_tmap(CUtensorMap *m, const void *ptr, uint64_t rows, uint64_t K, int es
 
 constexpr size_t gemm_stage_bytes(int BN) { return (size_t)(128 + BN) * 128; }
 
-/* resident CTAs per SM the stage ring is sized for: 1 (deep ring) or 2
- * (one CTA's epilogue overlaps the other's main loop); 0 = choose: 2,
- * except for split-K launches (few long-K tiles), which run best with 1 */
+/* kernel choice: 0 = automatic (the persistent kernel, or for split-K
+ * launches the per-tile kernel with its ring sized for one CTA per SM);
+ * 1 or 2 = the per-tile kernel with its ring sized for 1 or 2 resident
+ * CTAs per SM; 3 = the persistent kernel (split-K launches keep the
+ * per-tile one) */
 int g_gemm_ctas_per_sm = 0;
 
 }  // namespace
 
 int gemm_set_ctas_per_sm(int c) {
-  if (c < 0 || c > 2) return set_error(ZETA_ERR_ARG, "gemm: CTAs per SM must be 0 (auto), 1 or 2");
+  if (c < 0 || c > 3)
+    return set_error(ZETA_ERR_ARG, "gemm: 0 (auto), 1 or 2 (per-tile kernel, CTAs per SM) or 3 (persistent)");
   g_gemm_ctas_per_sm = c;
   return ZETA_OK;
 }
@@ -298,7 +466,28 @@ int gemm_launch(const GemmArgs &g, bool fp8, cudaStream_t s, int accumulate = 0)
   splits = (nkb + kbps - 1) / kbps;
   if (splits > 1 && accumulate == 2) ZCHECK(cudaMemsetAsync(g.Cf, 0, (size_t)g.M * g.N * sizeof(float), s));
   const size_t stage = gemm_stage_bytes(BN);
-  const int ctas = g_gemm_ctas_per_sm ? g_gemm_ctas_per_sm : (splits > 1 ? 1 : 2);
+  if (splits == 1 && (g_gemm_ctas_per_sm == 0 || g_gemm_ctas_per_sm == 3)) {
+    /* persistent: a 192 KB ring, one CTA per SM (at least 120 KB of
+     * shared memory each, so that two never share an SM's tensor memory) */
+    int pst = (int)((192 * 1024) / stage);
+    if (pst > kMaxStages) pst = kMaxStages;
+    const size_t psmem = std::max<size_t>(1024 + (size_t)pst * stage, 120 * 1024);
+    const int sms = ctx().sms > 0 ? ctx().sms : 148;
+    const int pgrid = std::min(mt * nt, sms);
+#define ZETA_GEMM_PCASE(BNV)                                                                              \
+  if (BN == BNV) {                                                                                        \
+    auto k = fp8 ? k_gemm_persist<BNV, true> : k_gemm_persist<BNV, false>;                                \
+    ZCHECK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psmem));              \
+    k<<<pgrid, kPersistThreads, psmem, s>>>(ta, tb, g, pst);                                              \
+  }
+    ZETA_GEMM_PCASE(64)
+    ZETA_GEMM_PCASE(128)
+    ZETA_GEMM_PCASE(256)
+#undef ZETA_GEMM_PCASE
+    ZCHECK(cudaGetLastError());
+    return ZETA_OK;
+  }
+  const int ctas = g_gemm_ctas_per_sm == 1 || g_gemm_ctas_per_sm == 2 ? g_gemm_ctas_per_sm : (splits > 1 ? 1 : 2);
   int stages = (int)((ctas == 2 ? 110 * 1024 : 200 * 1024) / stage);
   if (stages > kMaxStages) stages = kMaxStages;
   if (stages > nkb) stages = nkb < 2 ? 2 : nkb;

@@ -72,6 +72,11 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t phase, uint32_
   return false;
 }
 
+/* plain arrival (the barrier counts its arrivals) */
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
 /* arrive once and announce `bytes` of asynchronous transfers on `bar` */
 __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
