@@ -775,7 +775,8 @@ def run_gemm(args):
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device=dev)
     peaks = measured_peaks()
     rows = []
-    for (M, N, K) in GEMM_SHAPES:
+    pick = [int(x) for x in args.gemm_shapes.split(",")] if args.gemm_shapes else range(len(GEMM_SHAPES))
+    for (M, N, K) in [GEMM_SHAPES[i] for i in pick]:
         A = (torch.rand(M, K, device=dev, generator=g) - 0.5).to(torch.bfloat16)
         B = (torch.rand(N, K, device=dev, generator=g) - 0.5).to(torch.bfloat16)
         C = torch.empty(M, N, device=dev, dtype=torch.float32)
@@ -879,6 +880,7 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--n", type=int, default=0, help="positions per GPU (default: the workload's 4096)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the timed CPU baseline (profiling runs)")
+    ap.add_argument("--gemm-shapes", default="", help="gemm: comma-separated indices into GEMM_SHAPES (default all)")
     ap.add_argument("--all-promotions", action="store_true",
                     help="perft promotes to all four pieces (not the reference's rule: no CPU baseline or roofline)")
     ap.add_argument("--no-search", action="store_true",

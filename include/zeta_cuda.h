@@ -275,11 +275,12 @@ int zeta_mlp_scores(const uint64_t *boards, const uint8_t *stm, int n, int fp8, 
  * (fp8 != 0), device buffers, K a multiple of 64 (BF16) or 128 (FP8), N a
  * multiple of 16.  tcgen05.mma with FP32 accumulation in tensor memory. */
 int zeta_gemm_tc(const void *d_A, const void *d_B, float *d_C, int M, int N, int K, int fp8, void *stream);
-/* Kernel choice of the tensor-core products: 0 (default) the persistent
- * kernel -- one CTA per SM walks the output tiles with two tensor-memory
- * accumulators, so a tile's epilogue overlaps the next tile's MMAs -- and
- * for split-K launches (weight gradients) the per-tile kernel with its
- * shared-memory ring sized for one CTA per SM; 1 or 2 the per-tile kernel
+/* Kernel choice of the tensor-core products: 0 (default) for short K (at
+ * most 32 K slices of 128 bytes per tile, the network's shapes) the
+ * persistent kernel -- one CTA per SM walks the output tiles with two
+ * tensor-memory accumulators, so a tile's epilogue overlaps the next
+ * tile's MMAs -- else the per-tile kernel (its shared-memory ring sized
+ * for 2 CTAs per SM, or 1 for split-K launches such as weight gradients); 1 or 2 the per-tile kernel
  * with its ring sized for 1 or 2 resident CTAs per SM; 3 the persistent
  * kernel (split-K launches keep the per-tile one).  Results do not depend
  * on the choice. */

@@ -258,6 +258,7 @@ __global__ void __launch_bounds__(128, 1)
  * launch asks for enough shared memory that two CTAs never share an SM,
  * so the 2 x BN-column allocation never waits for another CTA. */
 constexpr int kPersistThreads = 192;
+constexpr int kPersistMaxSlices = 32; /* automatic choice: persistent up to this many K slices per tile */
 
 template <int BN, bool FP8>
 __global__ void __launch_bounds__(kPersistThreads, 1)
@@ -422,8 +423,10 @@ int make_tmap(CUtensorMap *m, const void *ptr, uint64_t rows, uint64_t K, int es
 
 constexpr size_t gemm_stage_bytes(int BN) { return (size_t)(128 + BN) * 128; }
 
-/* kernel choice: 0 = automatic (the persistent kernel, or for split-K
- * launches the per-tile kernel with its ring sized for one CTA per SM);
+/* kernel choice: 0 = automatic (the persistent kernel for short K -- up to
+ * kPersistMaxSlices K slices per tile, the network's shapes, where the
+ * epilogue is a large share of a tile's time -- else the per-tile kernel,
+ * its ring sized for 2 CTAs per SM, or 1 for split-K launches);
  * 1 or 2 = the per-tile kernel with its ring sized for 1 or 2 resident
  * CTAs per SM; 3 = the persistent kernel (split-K launches keep the
  * per-tile one) */
@@ -466,7 +469,7 @@ int gemm_launch(const GemmArgs &g, bool fp8, cudaStream_t s, int accumulate = 0)
   splits = (nkb + kbps - 1) / kbps;
   if (splits > 1 && accumulate == 2) ZCHECK(cudaMemsetAsync(g.Cf, 0, (size_t)g.M * g.N * sizeof(float), s));
   const size_t stage = gemm_stage_bytes(BN);
-  if (splits == 1 && (g_gemm_ctas_per_sm == 0 || g_gemm_ctas_per_sm == 3)) {
+  if (splits == 1 && (g_gemm_ctas_per_sm == 3 || (g_gemm_ctas_per_sm == 0 && nkb <= kPersistMaxSlices))) {
     /* persistent: a 192 KB ring, one CTA per SM (at least 120 KB of
      * shared memory each, so that two never share an SM's tensor memory) */
     int pst = (int)((192 * 1024) / stage);
