@@ -93,6 +93,42 @@ def test_host_board_layer_survives_malformed_fens(tmp_path):
         assert int(f[0]) == int(one_each), line
 
 
+MOVE_HARNESS = r"""
+#include <stdio.h>
+#include <string.h>
+#include "board.h"
+int main(void) {
+  char line[256];
+  while (fgets(line, sizeof line, stdin)) {
+    line[strcspn(line, "\n")] = 0;
+    printf("%d\n", move_text_ok(line) ? 1 : 0);
+  }
+  return 0;
+}
+"""
+
+MOVE_TEXT = {"e2e4": 1, "a7a8q": 1, "h2h1N": 1, "g1f3": 1, "e2e4x": 0, "e2e": 0, "": 0, "e9e4": 0, "i2e4": 0,
+             "e2e4qq": 0, "E2E4": 0, "e0e1": 0, "a7a8k": 0, "x" * 200: 0, "e2-e4": 0}
+
+
+def test_host_move_text_check(tmp_path):
+    """Coordinate move text the xboard loop accepts before it asks the
+    device for the position's legal moves: squares a-h / 1-8 and an
+    optional q, r, b or n; everything else is refused, under the
+    sanitizers."""
+    src = tmp_path / "m.c"
+    src.write_text(MOVE_HARNESS)
+    exe = tmp_path / "m_san"
+    r = subprocess.run(["gcc", "-O1", "-g", "-std=gnu11", "-fsanitize=address,undefined", "-fno-sanitize-recover=all",
+                        "-I", HOST, "-o", str(exe), str(src), os.path.join(HOST, "board.c")], capture_output=True)
+    if r.returncode != 0:
+        pytest.skip("sanitizer runtime not available: " + r.stderr.decode(errors="replace")[-200:])
+    texts = list(MOVE_TEXT)
+    out = subprocess.run([str(exe)], input="\n".join(texts) + "\n", capture_output=True, text=True, timeout=60)
+    assert out.returncode == 0, out.stderr[-2000:]
+    assert [int(x) for x in out.stdout.split()] == [MOVE_TEXT[t] for t in texts]
+
+
 CONFIG_HARNESS = r"""
 #include <inttypes.h>
 #include <stdio.h>
@@ -225,3 +261,22 @@ def test_zeta_xboard_session_plays_a_legal_move():
     b, s = ol.setboard("rnbqkbnr/pppppppp/8/8/4P3/8/PPPP1PPP/RNBQKBNR b KQkq - 0 1")
     legal = {ol.move2can(m) for m in ol.genmoves(b, s)}
     assert moves[0] in legal
+
+
+@pytest.mark.gpu
+def test_zeta_refuses_illegal_and_malformed_user_moves():
+    """`usermove` plays only a legal move of the position (the device's
+    generator lists them, under-promotions included): malformed text and
+    illegal moves are answered with "Illegal move" and leave the game as
+    it was; an under-promotion is played as the piece named."""
+    session = ("new\nforce\nusermove e2e5\nusermove e2\nusermove e7e5\nusermove e2e4\nusermove e7e5\n"
+               "setboard 4k3/1P6/8/8/8/8/8/4K3 w - - 0 1\nusermove b7b8n\nprint\nquit\n")
+    r = subprocess.run([ZETA], input=session, capture_output=True, text=True, timeout=300, cwd=ROOT)
+    assert r.returncode == 0, r.stderr
+    illegal = [l.split(":", 1)[1].strip() for l in r.stdout.splitlines() if l.startswith("Illegal move:")]
+    # e7e5 is illegal the first time (white to move), legal after e2e4
+    assert illegal == ["e2e5", "e2", "e7e5"], r.stdout
+    fen = [l[2:] for l in r.stdout.splitlines() if l.startswith("# ") and "/" in l][-1]
+    b, s = ol.setboard(fen)
+    want, ws = ol.setboard("1N2k3/8/8/8/8/8/8/4K3 b - - 0 1")
+    assert [int(x) for x in b[:4]] == [int(x) for x in want[:4]] and s == ws, fen

@@ -182,6 +182,15 @@ void move2can(Move m, char out[6]) {
   }
 }
 
+bool move_text_ok(const char *s) {
+  if (!s) return false;
+  const size_t n = strlen(s);
+  if (n != 4 && n != 5) return false;
+  for (int i = 0; i < 4; i += 2)
+    if (s[i] < 'a' || s[i] > 'h' || s[i + 1] < '1' || s[i + 1] > '8') return false;
+  return n == 4 || strchr("qrbnQRBN", s[4]) != NULL;
+}
+
 Move can2move(const char *s, const Bitboard b[7], int stm) {
   int from = (s[1] - '1') * 8 + (s[0] - 'a'), to = (s[3] - '1') * 8 + (s[2] - 'a');
   from &= 63;

@@ -56,6 +56,9 @@ void board_play(Bitboard board[7], int stm, Move move);
 /* move text, src/io.c:70-160 */
 void move2can(Move move, char out[6]);
 Move can2move(const char *can, const Bitboard board[7], int stm);
+/* true when `can` is coordinate move text: from and to squares (a-h,
+ * 1-8) and an optional promotion letter (q, r, b, n), nothing else */
+bool move_text_ok(const char *can);
 
 /* printboard, src/io.c:165-225 */
 void board_print(const Bitboard board[7], int stm);

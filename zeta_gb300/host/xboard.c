@@ -9,6 +9,7 @@
 #include <string.h>
 
 #include "../../include/clrun.h"
+#include "../../include/zeta_cuda.h"
 #include "engine.h"
 
 static bool xboard_mode = false, force_mode = false, post = true;
@@ -33,6 +34,31 @@ static void play_move(Move m) {
     HashHistory[PLY] = BOARD[QBBHASH];
     MoveHistory[PLY] = m;
   }
+}
+
+/* The legal move a user's move text names, or 0.  The text must be
+ * coordinate notation (move_text_ok); the position's legal moves come from
+ * the device's perft generator with all four promotions, and a promotion
+ * without a piece letter is taken as the queen's.  The reference plays
+ * whatever the text decodes to (src/xboard.c, usermove). */
+static Move legal_user_move(const char *mvs) {
+  if (!move_text_ok(mvs)) return 0;
+  const Move m = can2move(mvs, BOARD, STM);
+  uint32_t list[256];
+  int32_t n = 0;
+  const uint8_t side = (uint8_t)STM;
+  if (zeta_genmoves_batch(BOARD, &side, 1, 8, list, &n) != ZETA_OK) {
+    printf("Error (device): %s\n", zeta_last_error());
+    return 0;
+  }
+  for (int i = 0; i < n; i++) {
+    const Move g = list[i];
+    if (GETSQFROM(g) != GETSQFROM(m) || GETSQTO(g) != GETSQTO(m)) continue;
+    const int kind = GETPTO(g) >> 1, asked = GETPTO(m) >> 1;
+    if ((GETPFROM(g) >> 1) != PAWN || kind == PAWN) return g; /* not a promotion */
+    if (asked == kind || (asked == PAWN && kind == QUEEN)) return g;
+  }
+  return 0;
 }
 
 /* the node budget of a move from its time (src/xboard.c:193, 371) */
@@ -98,7 +124,11 @@ void xboard(void) {
     } else if (!strcmp(cmd, "usermove")) {
       char mvs[16] = {0};
       sscanf(arg, "%15s", mvs);
-      Move m = can2move(mvs, BOARD, STM);
+      const Move m = legal_user_move(mvs);
+      if (!m) {
+        printf("Illegal move: %s\n", mvs);
+        continue;
+      }
       play_move(m);
       if (!force_mode) think_and_move();
     } else if (!strcmp(cmd, "sd")) {
