@@ -282,11 +282,8 @@ def run_ours(args):
         "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(sum(step_ms) / len(step_ms), 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic (seeded random playouts)",
-        "config": {**perft_config(n), "leaves_per_step_per_gpu": int(ref_counts.sum()),
-                   "promotions": ("queen, rook, bishop, knight (not the reference's rule)" if args.all_promotions
-                                  else "queen only (the reference's rule)"),
-                   "l2": "flushed between timed steps (256 MB write)", "parallelism": f"replicas x{world}",
-                   "perft_config": z.perft_config()},
+        "config": perft_config(n, world, args.all_promotions),
+        "leaves_per_step_per_gpu": int(ref_counts.sum()), "perft_launch": z.perft_config(),
         "e2e": {"value": round(e2e_value, 1), "unit": UNIT, "h2d_bytes_per_step": n * 58,
                 "d2h_bytes_per_step": n * 8},
         "gpu_launches": 14 * args.steps,
@@ -500,10 +497,14 @@ def _ref_lib():
     return ol, ol.reference()
 
 
-def perft_config(n: int) -> dict:
-    """The batched-perft workload, as both arms of the bench name it."""
+def perft_config(n: int, world: int, all_promotions: bool = False) -> dict:
+    """The batched-perft workload, as both arms of the bench name it (the
+    same `config` object in both lines)."""
     return {"workload": f"{WORKLOAD}: {n} seeded playouts of 10-60 plies, perft depth U[3,5]",
-            "positions_per_gpu": n}
+            "positions_per_gpu": n,
+            "promotions": ("queen, rook, bishop, knight (not the reference's rule)" if all_promotions
+                           else "queen only (the reference's rule)"),
+            "l2": "flushed between timed GPU steps (256 MB write)", "parallelism": f"replicas x{world}"}
 
 
 def reference_sample_size(cores: int) -> int:
@@ -865,7 +866,7 @@ def run_reference(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t_total / args.steps * 1e3, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
         "data": "synthetic (seeded random playouts)",
-        "config": perft_config(w["n"]),
+        "config": perft_config(w["n"], world),
         "cpu_baseline": {"value": round(value, 1), "unit": UNIT, "cores": cores, "kind": "reference",
                          "sample": sample},
         "e2e": {"value": round(value, 1), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
