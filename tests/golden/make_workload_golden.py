@@ -12,7 +12,7 @@ perft_workload.json
 search_workload.json
     The batched-search workload (1024 playouts of 20-40 plies with at least
     20 pieces; seed 0x5A17A0000000001 + 3): the oracle's plain alpha-beta
-    root score at depth 7 (the configured depth) of the first 32 positions,
+    root score at depth 7 (the configured depth) of the first 128 positions,
     with the oracle's best move and visited nodes.  The value comes from
     zo_alphabeta_ordered, which is full-window alpha-beta with reordered
     moves; the script checks it against zo_alphabeta on every position at
@@ -53,7 +53,7 @@ sys.path.insert(0, os.path.dirname(HERE))
 SEED_BASE = 0x5A17A0000000001
 PERFT = dict(seed=SEED_BASE + 2, n=4096, min_plies=10, max_plies=60, min_pieces=0, min_depth=3, max_depth=5)
 SEARCH = dict(seed=SEED_BASE + 3, n=1024, min_plies=20, max_plies=40, min_pieces=20, min_depth=7, max_depth=7)
-SEARCH_FIXTURE_POSITIONS = 32
+SEARCH_FIXTURE_POSITIONS = 128
 SEARCH_DEPTH = 7
 
 

@@ -6,7 +6,7 @@ oracle and the reference kernel produced on host cores
   3-5 (55 G leaves): every count equal to the oracle's, and 16 of them
   (depths 4 and 5) equal to the reference perft kernel's own;
 * batched pure search at the configured depth 7 with the bench's table
-  (1 GiB) and launch settings: the first 32 root scores equal the oracle's
+  (1 GiB) and launch settings: the first 128 root scores equal the oracle's
   plain alpha-beta value.
 
 Positions come from the device generator; the fixture's SHA-256 of the
@@ -59,7 +59,7 @@ def test_perft_bench_batch_equals_oracle_at_full_size(zeta_device):
         assert int(got[c["index"]]) == c["leaves"] and int(depth[c["index"]]) == c["depth"], c
 
 
-@pytest.mark.parametrize("form,workers,helpers,n", [(3, 2, 64, 1024), (1, 32, 128, 32)])
+@pytest.mark.parametrize("form,workers,helpers,n", [(3, 2, 64, 1024), (1, 32, 128, 128)])
 def test_search_bench_batch_depth7_equals_oracle(zeta_device, form, workers, helpers, n):
     """The bench's settings: warp-cooperative 2 workers per position with a
     helper cap of 64 over the whole 1024-position batch, and the dense form
@@ -82,5 +82,6 @@ def test_search_bench_batch_depth7_equals_oracle(zeta_device, form, workers, hel
         z.search_set_helpers(0)
         z.release()
         z.init(0, 64, 16)
-    assert list(scores[:k]) == fx["scores"]
+    k = min(k, n)
+    assert list(scores[:k]) == fx["scores"][:k]
     assert (nodes[:n] > 0).all()
